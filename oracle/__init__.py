@@ -1,0 +1,161 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+The oracle restates the reference kNN self-join on the CPU (see
+knnsj_oracle.cpp for the file:line map).  Only the tests, the smoke check and
+bench.py's CPU-baseline leg import this module; the product library never
+does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libknnsj_oracle.so")
+_lib = None
+
+
+class OrcStats(ctypes.Structure):
+    _fields_ = [
+        ("avg_distance", ctypes.c_double),
+        ("bucket_width", ctypes.c_double),
+        ("eps0", ctypes.c_double),
+        ("eps_final", ctypes.c_double),
+        ("total_distance", ctypes.c_double),
+        ("pair_count", ctypes.c_uint64),
+        ("candidates", ctypes.c_uint64),
+        ("bucket", ctypes.c_int32),
+        ("iterations", ctypes.c_int32),
+        ("reindexes", ctypes.c_int32),
+        ("eps_offset", ctypes.c_uint32),
+        ("eps_sample_blocks", ctypes.c_uint32),
+        ("perm", ctypes.c_uint32 * 64),
+    ]
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(_LIB_PATH):
+        subprocess.check_call(["bash", os.path.join(_HERE, "build_oracle.sh")])
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(_LIB_PATH)
+    return _lib
+
+
+def _sfx(dtype) -> str:
+    dt = np.dtype(dtype)
+    if dt == np.float32:
+        return "f32"
+    if dt == np.float64:
+        return "f64"
+    raise TypeError(f"unsupported dtype {dt}")
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
+
+
+def reorder(data: np.ndarray):
+    """Dimension order of ReorderByDimension (main.cu:2521) and variances."""
+    data = np.ascontiguousarray(data)
+    n, d = data.shape
+    perm = np.zeros(d, np.uint32)
+    var = np.zeros(d, data.dtype)
+    f = getattr(lib(), "orc_reorder_" + _sfx(data.dtype))
+    rc = f(_ptr(data), ctypes.c_uint64(n), ctypes.c_uint32(d), _ptr(perm), _ptr(var))
+    assert rc == 0
+    return perm, var
+
+
+def estimate_eps(data_reordered: np.ndarray, k: int, beta: float, nthreads: int = 0):
+    """Epsilon estimator (GPU.cu:3088) on already-reordered data."""
+    x = np.ascontiguousarray(data_reordered)
+    n, d = x.shape
+    out = np.zeros(6, np.float64)
+    hist = np.zeros(10000, np.uint32)
+    f = getattr(lib(), "orc_eps_" + _sfx(x.dtype))
+    rc = f(_ptr(x), ctypes.c_uint64(n), ctypes.c_uint32(d), ctypes.c_uint32(k),
+           ctypes.c_double(beta), _ptr(out), _ptr(hist), ctypes.c_int(nthreads))
+    assert rc == 0
+    return {
+        "avg": out[0], "bucket_width": out[1], "eps0": out[2], "bucket": int(out[3]),
+        "pair_count": int(out[4]), "offset": int(out[5]), "hist": hist,
+    }
+
+
+def grid(data_reordered: np.ndarray, di: int, eps: float, nthreads: int = 0):
+    """Grid index at cell width eps (GPU.cu:3715 / main.cu:1968)."""
+    x = np.ascontiguousarray(data_reordered)
+    n, d = x.shape
+    T = x.dtype.type
+    minArr = np.zeros(di, x.dtype)
+    nCells = np.zeros(di, np.uint32)
+    total = ctypes.c_uint64(0)
+    keys = np.zeros(n, np.uint64)
+    imin = np.zeros(n, np.int32)
+    imax = np.zeros(n, np.int32)
+    lookup = np.zeros(n, np.uint32)
+    nne = ctypes.c_uint64(0)
+    f = getattr(lib(), "orc_grid_" + _sfx(x.dtype))
+    epsc = ctypes.c_float(eps) if x.dtype == np.float32 else ctypes.c_double(eps)
+    rc = f(_ptr(x), ctypes.c_uint64(n), ctypes.c_uint32(d), ctypes.c_uint32(di), epsc,
+           _ptr(minArr), _ptr(nCells), ctypes.byref(total), _ptr(keys), _ptr(imin),
+           _ptr(imax), _ptr(lookup), ctypes.byref(nne), ctypes.c_int(nthreads))
+    assert rc == 0
+    c = nne.value
+    return {
+        "minArr": minArr, "nCells": nCells, "totalCells": total.value,
+        "cellKeys": keys[:c].copy(), "indexmin": imin[:c].copy(),
+        "indexmax": imax[:c].copy(), "lookup": lookup,
+    }
+
+
+def join(data: np.ndarray, k: int, di: int = 0, beta: float = 0.05, reorder: bool = True,
+         queries=None, max_iterations: int = 0, nthreads: int = 0):
+    """Reference pipeline (main.cu:109-510).  Returns (rc, ids, dists, stats).
+
+    ids / dists are (N, k+1); rows of queries not processed stay -1 / 0.
+    """
+    x = np.ascontiguousarray(data)
+    n, d = x.shape
+    K = k + 1
+    ids = np.full((n, K), -1, np.int32)
+    dists = np.zeros((n, K), x.dtype)
+    st = OrcStats()
+    if queries is None:
+        qp, nq = None, 0
+    else:
+        q = np.ascontiguousarray(queries, dtype=np.uint32)
+        qp, nq = _ptr(q), q.size
+    f = getattr(lib(), "orc_join_" + _sfx(x.dtype))
+    rc = f(_ptr(x), ctypes.c_uint64(n), ctypes.c_uint32(d), ctypes.c_uint32(k),
+           ctypes.c_int32(di), ctypes.c_double(beta), ctypes.c_int32(1 if reorder else 0),
+           qp, ctypes.c_uint64(nq), ctypes.c_int32(max_iterations), _ptr(ids), _ptr(dists),
+           ctypes.byref(st), ctypes.c_int(nthreads))
+    return rc, ids, dists, st
+
+
+def bruteforce(data_summation_order: np.ndarray, K: int, queries, nthreads: int = 0):
+    """First K points by (acc, id) for each query, over all points."""
+    x = np.ascontiguousarray(data_summation_order)
+    n, d = x.shape
+    q = np.ascontiguousarray(queries, dtype=np.uint32)
+    ids = np.zeros((q.size, K), np.int32)
+    dists = np.zeros((q.size, K), x.dtype)
+    f = getattr(lib(), "orc_bruteforce_" + _sfx(x.dtype))
+    rc = f(_ptr(x), ctypes.c_uint64(n), ctypes.c_uint32(d), ctypes.c_uint32(K), _ptr(q),
+           ctypes.c_uint64(q.size), _ptr(ids), _ptr(dists), ctypes.c_int(nthreads))
+    assert rc == 0
+    return ids, dists
