@@ -1,0 +1,334 @@
+// api.cu -- the C ABI (include/knnsj.h): KNNJoinPy and the status-returning
+// entry points.  Validation, defaults, device selection, host<->device
+// staging and error translation live here; the join itself is run_join
+// (join.cu).
+
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#ifdef KNNSJ_BUILD_DTYPE_DOUBLE
+#define KNNSJ_KNNJOINPY_DOUBLE 1
+#endif
+#include "knnsj_host.h"
+#include "knnsj_internal.h"
+
+#ifndef KNNSJ_BUILD_DTYPE_DOUBLE
+typedef float knnjoinpy_t;
+#define KNNSJ_PY_DTYPE KNNSJ_F32
+#else
+typedef double knnjoinpy_t;
+#define KNNSJ_PY_DTYPE KNNSJ_F64
+#endif
+
+using namespace knnsj;
+
+namespace {
+
+std::mutex g_call_mutex;
+
+const char* env(const char* name) {
+  const char* v = std::getenv(name);
+  return (v && *v) ? v : nullptr;
+}
+
+knnsj_status make_config(const knnsj_options* o, uint32_t d, JoinConfig* c) {
+  // params.h defaults, then environment, then explicit options
+  c->beta = 0.05;
+  c->num_indexed_dims = d < 6 ? d : 6;
+  if (const char* e = env("KNNSJ_BETA")) c->beta = std::atof(e);
+  if (const char* e = env("KNNSJ_NUMINDEXEDDIM")) c->num_indexed_dims = (uint32_t)std::atoi(e);
+  if (const char* e = env("KNNSJ_VERBOSE")) c->verbose = std::atoi(e);
+  if (const char* e = env("KNNSJ_DENSE")) c->dense_mode = std::atoi(e);
+  if (o) {
+    if (o->struct_size < sizeof(uint32_t)) return KNNSJ_ERR_INVALID_ARGUMENT;
+    if (o->num_indexed_dims > 0) c->num_indexed_dims = (uint32_t)o->num_indexed_dims;
+    if (o->beta >= 0) c->beta = o->beta;
+    c->no_reorder = o->no_reorder;
+    c->radius_mode = o->radius_mode;
+    c->max_iterations = o->max_iterations;
+    if (o->verbose) c->verbose = o->verbose;
+  }
+  if (c->num_indexed_dims == 0 || c->num_indexed_dims > d) c->num_indexed_dims = d < 6 ? d : 6;
+  if (c->num_indexed_dims > (uint32_t)MAX_DI) return KNNSJ_ERR_UNSUPPORTED;
+  if (!(c->beta >= 0.0) || !(c->beta <= 1.0)) return KNNSJ_ERR_INVALID_ARGUMENT;
+  if (c->radius_mode != KNNSJ_RADIUS_BETA && c->radius_mode != KNNSJ_RADIUS_LEARNED)
+    return KNNSJ_ERR_INVALID_ARGUMENT;
+  return KNNSJ_OK;
+}
+
+knnsj_status validate(const void* data, uint64_t n, uint32_t d, uint32_t k, const void* ids,
+                      const void* dists) {
+  if (!data || !ids || !dists) return KNNSJ_ERR_INVALID_ARGUMENT;
+  if (n == 0 || d == 0 || d > (uint32_t)MAX_D) return KNNSJ_ERR_INVALID_ARGUMENT;
+  if (n >= (1ull << 31)) return KNNSJ_ERR_TOO_MANY_POINTS;
+  if ((uint64_t)k + 1 > n) return KNNSJ_ERR_K_TOO_LARGE;
+  if (k + 1 > 2048) return KNNSJ_ERR_UNSUPPORTED;
+  return KNNSJ_OK;
+}
+
+int select_device(const knnsj_options* o) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    throw StatusError{KNNSJ_ERR_NO_DEVICE, "no CUDA device"};
+  }
+  int dev = 0;
+  if (o && o->device >= 0) {
+    if (o->device >= count) throw StatusError{KNNSJ_ERR_INVALID_ARGUMENT, "device ordinal"};
+    dev = o->device;
+    KNNSJ_CUDA(cudaSetDevice(dev));
+  } else {
+    KNNSJ_CUDA(cudaGetDevice(&dev));
+  }
+  return dev;
+}
+
+Workspace& ready_workspace(int dev) {
+  Workspace& w = workspace(dev);
+  w.ensure_stream();
+  if (!w.sm_count) KNNSJ_CUDA(cudaDeviceGetAttribute(&w.sm_count, cudaDevAttrMultiProcessorCount, dev));
+  return w;
+}
+
+bool is_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+template <typename F>
+knnsj_status guarded(F&& f, knnsj_stats* st) {
+  try {
+    f();
+    return KNNSJ_OK;
+  } catch (const StatusError& e) {
+    if (std::getenv("KNNSJ_VERBOSE")) fprintf(stderr, "knnsj: %s\n", e.what);
+    return e.st;
+  } catch (const CudaError& e) {
+    fprintf(stderr, "knnsj: CUDA error %s in %s\n", cudaGetErrorString(e.err), e.where);
+    cudaGetLastError();
+    if (e.err == cudaErrorMemoryAllocation) return KNNSJ_ERR_OUT_OF_MEMORY;
+    return KNNSJ_ERR_CUDA;
+  } catch (const std::bad_alloc&) {
+    return KNNSJ_ERR_OUT_OF_MEMORY;
+  }
+  (void)st;
+}
+
+void init_stats(knnsj_stats* st) {
+  if (!st) return;
+  const uint32_t sz = st->struct_size;
+  std::memset(st, 0, sizeof(*st));
+  st->struct_size = sz ? sz : (uint32_t)sizeof(*st);
+}
+
+template <typename T>
+void host_join(const T* data, uint64_t n, uint32_t d, uint32_t k, const JoinConfig& cfg, int dev,
+               int32_t* out_ids, T* out_d, knnsj_stats* st) {
+  Workspace& w = ready_workspace(dev);
+  cudaStream_t s = w.stream;
+  const uint64_t K = (uint64_t)k + 1;
+  T* din = (T*)w.in.get(n * d * sizeof(T));
+  int32_t* dids = (int32_t*)w.ids.get(n * K * 4);
+  T* ddist = (T*)w.dists.get(n * K * sizeof(T));
+  cudaEvent_t t0, t1;
+  KNNSJ_CUDA(cudaEventCreate(&t0));
+  KNNSJ_CUDA(cudaEventCreate(&t1));
+  KNNSJ_CUDA(cudaEventRecord(t0, s));
+  KNNSJ_CUDA(cudaMemcpyAsync(din, data, n * d * sizeof(T), cudaMemcpyHostToDevice, s));
+  KNNSJ_CUDA(cudaEventRecord(t1, s));
+  run_join<T>(w, cfg, din, data, n, d, k, dids, ddist, st, s);
+  cudaEvent_t t2, t3;
+  KNNSJ_CUDA(cudaEventCreate(&t2));
+  KNNSJ_CUDA(cudaEventCreate(&t3));
+  KNNSJ_CUDA(cudaEventRecord(t2, s));
+  KNNSJ_CUDA(cudaMemcpyAsync(out_ids, dids, n * K * 4, cudaMemcpyDeviceToHost, s));
+  KNNSJ_CUDA(cudaMemcpyAsync(out_d, ddist, n * K * sizeof(T), cudaMemcpyDeviceToHost, s));
+  KNNSJ_CUDA(cudaEventRecord(t3, s));
+  KNNSJ_CUDA(cudaStreamSynchronize(s));
+  if (st) {
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, t0, t1);
+    cudaEventElapsedTime(&b, t2, t3);
+    st->ms_transfer = a + b;
+    // verification sum (GPU.cu:3690-3693), row-major
+    double tot = 0.0;
+    for (uint64_t i = 0; i < n * K; i++) {
+      const T sq = out_d[i] * out_d[i];
+      tot += sq;
+    }
+    st->total_distance = tot;
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaEventDestroy(t2);
+  cudaEventDestroy(t3);
+  if (cfg.verbose && st)
+    fprintf(stderr,
+            "knnsj: n=%llu d=%u k=%u eps0=%g bucket=%d iterations=%d regrids=%d candidates=%llu "
+            "prep=%.3f ms search=%.3f ms transfer=%.3f ms\n",
+            (unsigned long long)n, d, k, st->eps0, st->eps_bucket, st->iterations, st->regrids,
+            (unsigned long long)st->candidates, st->ms_prep, st->ms_search, st->ms_transfer);
+}
+
+template <typename T>
+void device_join(const T* data, uint64_t n, uint32_t d, uint32_t k, const JoinConfig& cfg, int dev,
+                 int32_t* out_ids, T* out_d, knnsj_stats* st) {
+  Workspace& w = ready_workspace(dev);
+  run_join<T>(w, cfg, data, nullptr, n, d, k, out_ids, out_d, st, w.stream);
+  KNNSJ_CUDA(cudaStreamSynchronize(w.stream));
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* knnsj_version(void) { return "knnsj 1.0 (sm_103a)"; }
+
+const char* knnsj_status_string(knnsj_status s) {
+  switch (s) {
+    case KNNSJ_OK: return "ok";
+    case KNNSJ_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case KNNSJ_ERR_DIM_MISMATCH: return "number of dimensions differs from GPUNUMDIM";
+    case KNNSJ_ERR_K_TOO_LARGE: return "k+1 exceeds the number of points";
+    case KNNSJ_ERR_NONFINITE_INPUT: return "NaN or infinite coordinate";
+    case KNNSJ_ERR_TOO_MANY_POINTS: return "more than 2^31-1 points";
+    case KNNSJ_ERR_NO_CONVERGENCE: return "iteration cap reached";
+    case KNNSJ_ERR_CUDA: return "CUDA error";
+    case KNNSJ_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case KNNSJ_ERR_NO_DEVICE: return "no CUDA device";
+    case KNNSJ_ERR_UNSUPPORTED: return "unsupported configuration";
+    case KNNSJ_ERR_IO: return "file I/O error";
+  }
+  return "unknown status";
+}
+
+knnsj_dtype knnsj_build_dtype(void) { return KNNSJ_PY_DTYPE; }
+
+knnsj_status knnsj_selfjoin(const void* data, knnsj_dtype dtype, uint64_t n, uint32_t d, uint32_t k,
+                            const knnsj_options* opts, int32_t* out_ids, void* out_dists,
+                            knnsj_stats* stats) {
+  knnsj_status v = validate(data, n, d, k, out_ids, out_dists);
+  if (v != KNNSJ_OK) return v;
+  if (dtype != KNNSJ_F32 && dtype != KNNSJ_F64) return KNNSJ_ERR_INVALID_ARGUMENT;
+  JoinConfig cfg;
+  v = make_config(opts, d, &cfg);
+  if (v != KNNSJ_OK) return v;
+  std::lock_guard<std::mutex> lock(g_call_mutex);
+  init_stats(stats);
+  return guarded(
+      [&] {
+        const int dev = select_device(opts);
+        if (dtype == KNNSJ_F32)
+          host_join<float>((const float*)data, n, d, k, cfg, dev, out_ids, (float*)out_dists, stats);
+        else
+          host_join<double>((const double*)data, n, d, k, cfg, dev, out_ids, (double*)out_dists, stats);
+      },
+      stats);
+}
+
+knnsj_status knnsj_selfjoin_device(const void* d_data, knnsj_dtype dtype, uint64_t n, uint32_t d,
+                                   uint32_t k, const knnsj_options* opts, int32_t* d_out_ids,
+                                   void* d_out_dists, knnsj_stats* stats) {
+  knnsj_status v = validate(d_data, n, d, k, d_out_ids, d_out_dists);
+  if (v != KNNSJ_OK) return v;
+  if (dtype != KNNSJ_F32 && dtype != KNNSJ_F64) return KNNSJ_ERR_INVALID_ARGUMENT;
+  JoinConfig cfg;
+  v = make_config(opts, d, &cfg);
+  if (v != KNNSJ_OK) return v;
+  std::lock_guard<std::mutex> lock(g_call_mutex);
+  init_stats(stats);
+  return guarded(
+      [&] {
+        const int dev = select_device(opts);
+        if (dtype == KNNSJ_F32)
+          device_join<float>((const float*)d_data, n, d, k, cfg, dev, d_out_ids, (float*)d_out_dists, stats);
+        else
+          device_join<double>((const double*)d_data, n, d, k, cfg, dev, d_out_ids, (double*)d_out_dists,
+                              stats);
+      },
+      stats);
+}
+
+knnsj_status knnsj_selfjoin_batched(uint32_t n_sets, knnsj_set* sets, knnsj_dtype dtype,
+                                    const knnsj_options* opts, knnsj_stats* stats) {
+  if (n_sets > 0 && !sets) return KNNSJ_ERR_INVALID_ARGUMENT;
+  knnsj_status first = KNNSJ_OK;
+  knnsj_stats agg;
+  std::memset(&agg, 0, sizeof(agg));
+  for (uint32_t i = 0; i < n_sets; i++) {
+    knnsj_stats one;
+    std::memset(&one, 0, sizeof(one));
+    one.struct_size = sizeof(one);
+    sets[i].status = knnsj_selfjoin(sets[i].data, dtype, sets[i].n, sets[i].d, sets[i].k, opts,
+                                    sets[i].out_ids, sets[i].out_dists, &one);
+    if (sets[i].status != KNNSJ_OK && first == KNNSJ_OK) first = sets[i].status;
+    agg.iterations += one.iterations;
+    agg.candidates += one.candidates;
+    agg.queries_run += one.queries_run;
+    agg.ms_total += one.ms_total;
+    agg.ms_prep += one.ms_prep;
+    agg.ms_search += one.ms_search;
+    agg.ms_transfer += one.ms_transfer;
+  }
+  if (stats) {
+    agg.struct_size = stats->struct_size ? stats->struct_size : (uint32_t)sizeof(agg);
+    *stats = agg;
+  }
+  return first;
+}
+
+void knnsj_release(void) {
+  std::lock_guard<std::mutex> lock(g_call_mutex);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  workspace(dev).release_all();
+}
+
+// KNNJoinPy (main.cu:514): same symbol and arguments; returns nothing.
+void KNNJoinPy(knnjoinpy_t* dataset, unsigned int NUMPOINTS, unsigned int kNN, unsigned int NDIM,
+               int* outNearestNeighborTable, knnjoinpy_t* outNearestNeighborTableDistances) {
+#ifdef GPUNUMDIM
+  if (GPUNUMDIM != NDIM) {
+    // main.cu:526-530
+    printf(
+        "\nERROR: The number of dimensions defined for the GPU is not the same as the number of "
+        "dimensions\n \t\t passed from the Python Interface. GPUNUMDIM=%d, NDIM=%d Exiting!!!",
+        GPUNUMDIM, NDIM);
+    return;
+  }
+#endif
+  knnsj_options o;
+  std::memset(&o, 0, sizeof(o));
+  o.struct_size = sizeof(o);
+  o.beta = -1.0;
+  o.device = -1;
+#ifdef NUMINDEXEDDIM
+  o.num_indexed_dims = NUMINDEXEDDIM;
+#endif
+#ifdef BETA
+  o.beta = BETA;
+#endif
+  knnsj_stats st;
+  std::memset(&st, 0, sizeof(st));
+  st.struct_size = sizeof(st);
+  const knnsj_status s = knnsj_selfjoin(dataset, KNNSJ_PY_DTYPE, NUMPOINTS, NDIM, kNN, &o,
+                                        outNearestNeighborTable, outNearestNeighborTableDistances, &st);
+  if (s != KNNSJ_OK) {
+    printf("\nERROR: knnsj: %s\n", knnsj_status_string(s));
+    return;
+  }
+  // main.cu:851 prints the same checksum line
+  printf("\n[Verification] Total distance (without sqaure root): %f", st.total_distance);
+  fflush(stdout);
+}
+
+}  // extern "C"

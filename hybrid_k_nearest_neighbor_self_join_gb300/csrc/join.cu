@@ -1,0 +1,350 @@
+// join.cu -- the self-join pipeline on one GPU.
+//
+// Host side of the reference's main()/KNNJoinPy (main.cu:109-510, 514-907),
+// re-planned for one resident dataset:
+//   1. dimension order (ReorderByDimension, main.cu:2521-2615) on the host,
+//      from every 100th point, in the reference's float/double arithmetic;
+//   2. one transpose into column arrays in that order (device);
+//   3. eps0 from BETA (sampleNeighborsBruteForce, GPU.cu:3088-3566);
+//   4. grid dimensions (generateNDGridDimensions, main.cu:2425-2488) and the
+//      grid index at width eps0 (populateNDGridIndexAndLookupArrayGPU,
+//      GPU.cu:3715-4067), built once and kept in HBM;
+//   5. the retry loop (main.cu:312-430): search all queries at eps0, then the
+//      failed ones at eps0 + m*eps0/2 over the widened cell ring of the same
+//      grid.  The reference repeats a pass at an unchanged radius when at
+//      most 25% failed (main.cu:330); that pass cannot succeed, so here the
+//      radius grows every pass.  When the ring would need many more cells
+//      than 3^NUMINDEXEDDIM, the grid is rebuilt at the current radius, as
+//      the reference does on every growth (main.cu:353).
+// Every device buffer lives in a per-device workspace reused across calls.
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "knnsj_internal.h"
+#include "knnsj_host.h"
+
+namespace knnsj {
+
+void* DevBuf::get(size_t need) {
+  if (need == 0) need = 16;
+  if (need > bytes) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, need);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      throw StatusError{KNNSJ_ERR_OUT_OF_MEMORY, "cudaMalloc"};
+    }
+    bytes = need;
+  }
+  return p;
+}
+
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+Workspace& workspace(int device) {
+  static std::vector<Workspace*> all;
+  static std::mutex m;
+  std::lock_guard<std::mutex> g(m);
+  if ((int)all.size() <= device) all.resize(device + 1, nullptr);
+  if (!all[device]) all[device] = new Workspace();
+  return *all[device];
+}
+
+void Workspace::release_all() {
+  DevBuf* bufs[] = {&in, &ids, &dists, &xs, &ps, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
+                    &scan_tmp, &flags, &pos, &ckeys, &coff, &dstart, &list0, &list1, &small,
+                    &eps_partial, &eps_pcount, &perm, &minmax_part, &qradius};
+  for (DevBuf* b : bufs) b->release();
+  if (stream) cudaStreamDestroy(stream);
+  stream = nullptr;
+  for (auto& e : ev) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
+  pinned_release();
+}
+
+void Workspace::pinned_release() {
+  if (h_pinned) cudaFreeHost(h_pinned);
+  h_pinned = nullptr;
+  h_pinned_bytes = 0;
+}
+
+void* Workspace::pinned(size_t need) {
+  if (need > h_pinned_bytes) {
+    pinned_release();
+    KNNSJ_CUDA(cudaMallocHost(&h_pinned, need));
+    h_pinned_bytes = need;
+  }
+  return h_pinned;
+}
+
+void Workspace::ensure_stream() {
+  if (!stream) KNNSJ_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  for (auto& e : ev)
+    if (!e) KNNSJ_CUDA(cudaEventCreate(&e));
+}
+
+namespace {
+
+struct SmallDev {  // layout of Workspace::small
+  uint32_t nonfinite;
+  uint32_t fail_count;
+  uint32_t work_counter;
+  uint32_t pad;
+  unsigned long long C;
+  unsigned long long cand;
+  double avg[2];
+  uint32_t hist[10000];
+};
+
+template <typename T>
+T host_fallback_eps(const std::vector<T>& mn, const std::vector<T>& mx, uint64_t n, uint32_t K) {
+  double ext = 0.0;
+  for (size_t j = 0; j < mn.size(); j++) ext = std::max(ext, (double)mx[j] - (double)mn[j]);
+  if (!(ext > 0)) return (T)1;
+  const double per_dim = std::max(1.0, std::floor(std::pow((double)n / K, 1.0 / mn.size())));
+  return (T)(ext / per_dim);
+}
+
+}  // namespace
+
+template <typename T>
+static void build_grid(Workspace& w, const JoinConfig& cfg, uint64_t n, uint32_t d, uint32_t di,
+                       const std::vector<T>& mn, const std::vector<T>& mx, T width, DeviceGrid<T>* out,
+                       cudaStream_t s) {
+  // generateNDGridDimensions (main.cu:2425-2488), in DTYPE.
+  GridGeom<T> g{};
+  g.di = di;
+  g.width = width;
+  unsigned long long mult = 1;
+  bool overflow = false;
+  for (uint32_t j = 0; j < di; j++) {
+    const T lo = mn[j] - width;
+    const T hi = mx[j] + width;
+    const T cells = std::ceil((hi - lo) / width);
+    if (!(cells < 4294967295.0)) throw StatusError{KNNSJ_ERR_UNSUPPORTED, "grid too fine"};
+    g.minv[j] = lo;
+    g.ncell[j] = (uint32_t)cells;
+    if (g.ncell[j] == 0) g.ncell[j] = 1;
+    g.mult[j] = mult;
+    if (mult > ~0ull / g.ncell[j]) overflow = true;
+    mult *= g.ncell[j];
+  }
+  if (overflow) throw StatusError{KNNSJ_ERR_UNSUPPORTED, "more than 2^64 grid cells"};
+  g.total_cells = mult;
+  int bits = 0;
+  while (bits < 64 && ((mult - 1) >> bits) != 0) bits++;
+
+  GridScratch sc;
+  sc.keys[0] = (unsigned long long*)w.keys0.get(n * 8);
+  sc.keys[1] = (unsigned long long*)w.keys1.get(n * 8);
+  sc.vals[0] = (uint32_t*)w.vals0.get(n * 4);
+  sc.vals[1] = (uint32_t*)w.vals1.get(n * 4);
+  sc.hist_elems = radix_hist_elems(n);
+  sc.hist = (uint32_t*)w.hist.get(sc.hist_elems * 4);
+  sc.scan_tmp_elems = scan_tmp_elems(std::max<size_t>(sc.hist_elems, n + 1));
+  sc.scan_tmp = (uint32_t*)w.scan_tmp.get(sc.scan_tmp_elems * 4);
+  const T* xs = (const T*)w.xs.p;
+  launch_cell_ids<T>(xs, n, g, sc.keys[0], sc.vals[0], s);
+  const int cur = radix_sort_pairs(sc, n, bits, s);
+  const unsigned long long* skeys = sc.keys[cur];
+  const uint32_t* sids = sc.vals[cur];
+  uint32_t* flags = (uint32_t*)w.flags.get(n * 4);
+  uint32_t* pos = (uint32_t*)w.pos.get(n * 4);
+  unsigned long long* ckeys = (unsigned long long*)w.ckeys.get(n * 8);
+  uint32_t* coff = (uint32_t*)w.coff.get((n + 1) * 4);
+  SmallDev* sm = (SmallDev*)w.small.p;
+  launch_compact_cells(skeys, n, flags, pos, sc.scan_tmp, ckeys, coff, &sm->C, s);
+  T* ps = (T*)w.ps.get(n * d * sizeof(T));
+  uint32_t* pid = (uint32_t*)w.pid.get(n * 4);
+  KNNSJ_CUDA(cudaMemcpyAsync(pid, sids, n * 4, cudaMemcpyDeviceToDevice, s));
+  launch_gather_sorted<T>(xs, n, d, sids, ps, s);
+  unsigned long long C = 0;
+  KNNSJ_CUDA(cudaMemcpyAsync(&C, &sm->C, sizeof(C), cudaMemcpyDeviceToHost, s));
+  KNNSJ_CUDA(cudaStreamSynchronize(s));
+  out->geom = g;
+  out->ps = ps;
+  out->pid = pid;
+  out->ckeys = ckeys;
+  out->coff = coff;
+  out->C = C;
+  const unsigned long long dense_limit = std::max<unsigned long long>(4ull * n, 1ull << 24);
+  out->dense = (cfg.dense_mode != 0) && (g.total_cells <= dense_limit) && g.total_cells < (1ull << 31);
+  if (cfg.dense_mode == 2) out->dense = g.total_cells < (1ull << 31);
+  out->dstart = nullptr;
+  if (out->dense) {
+    uint32_t* dstart = (uint32_t*)w.dstart.get((g.total_cells + 1) * 4);
+    launch_dense_table(ckeys, coff, C, g.total_cells, dstart, s);
+    out->dstart = dstart;
+  }
+}
+
+// Cells per dimension a ring of radius r spans on a grid of width w.
+static double ring_rows(double r, double w, uint32_t di) {
+  const double per = 2.0 * r / w + 1.0;
+  return std::pow(per, (double)(di > 0 ? di - 1 : 0));
+}
+
+template <typename T>
+void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
+              uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s) {
+  const uint32_t K = k + 1;
+  const uint32_t di = cfg.num_indexed_dims;
+  cudaEvent_t* ev = w.ev;
+  KNNSJ_CUDA(cudaEventRecord(ev[0], s));
+
+  // 1. dimension order
+  std::vector<uint32_t> perm(d);
+  for (uint32_t j = 0; j < d; j++) perm[j] = j;
+  if (!cfg.no_reorder) {
+    const uint64_t ns = (n + 99) / 100;
+    std::vector<T> sample(ns * d);
+    if (h_aos) {
+      for (uint64_t i = 0; i < ns; i++)
+        std::memcpy(&sample[i * d], h_aos + i * 100 * d, d * sizeof(T));
+    } else {
+      KNNSJ_CUDA(cudaMemcpy2DAsync(sample.data(), d * sizeof(T), d_aos, 100 * d * sizeof(T),
+                                   d * sizeof(T), ns, cudaMemcpyDeviceToHost, s));
+      KNNSJ_CUDA(cudaStreamSynchronize(s));
+    }
+    reorder_from_sample<T>(sample.data(), ns, n, d, perm.data(), nullptr);
+  }
+  if (st)
+    for (uint32_t j = 0; j < d && j < 64; j++) st->perm[j] = perm[j];
+
+  // 2. transpose into column arrays
+  uint32_t* d_perm = (uint32_t*)w.perm.get(d * 4);
+  SmallDev* sm = (SmallDev*)w.small.get(sizeof(SmallDev));
+  KNNSJ_CUDA(cudaMemsetAsync(sm, 0, offsetof(SmallDev, hist), s));
+  KNNSJ_CUDA(cudaMemcpyAsync(d_perm, perm.data(), d * 4, cudaMemcpyHostToDevice, s));
+  T* xs = (T*)w.xs.get(n * d * sizeof(T));
+  launch_transpose_reorder<T>(d_aos, xs, n, d, d_perm, s, &sm->nonfinite);
+  T* mm_part = (T*)w.minmax_part.get(1024 * 2 * di * sizeof(T) + 2 * di * sizeof(T));
+  T* d_minmax = mm_part + 1024 * 2 * di;
+  launch_minmax<T>(xs, n, di, d_minmax, mm_part, s);
+
+  // 3. eps0 (GPU.cu:3088-3566)
+  EpsScratch es;
+  const uint64_t nthr = eps_avg_threads(n);
+  es.partial = (double*)w.eps_partial.get(std::max<uint64_t>(nthr, 1) * 8);
+  es.pcount = (unsigned long long*)w.eps_pcount.get(std::max<uint64_t>(nthr, 1) * 8);
+  es.avg_out = sm->avg;
+  es.hist = sm->hist;
+  launch_eps<T>(xs, n, d, es, s);
+  std::vector<uint8_t> hsmall(sizeof(SmallDev));
+  std::vector<T> hmm(2 * di);
+  KNNSJ_CUDA(cudaMemcpyAsync(hmm.data(), d_minmax, 2 * di * sizeof(T), cudaMemcpyDeviceToHost, s));
+  KNNSJ_CUDA(cudaMemcpyAsync(hsmall.data(), sm, sizeof(SmallDev), cudaMemcpyDeviceToHost, s));
+  KNNSJ_CUDA(cudaStreamSynchronize(s));
+  const SmallDev* hs = (const SmallDev*)hsmall.data();
+  if (hs->nonfinite) throw StatusError{KNNSJ_ERR_NONFINITE_INPUT, "NaN or infinite coordinate"};
+  const EpsChoice ec = choose_eps(hs->hist, hs->avg[0], n, k, cfg.beta);
+  T eps0 = (T)ec.eps;
+  std::vector<T> mn(di), mx(di);
+  for (uint32_t j = 0; j < di; j++) {
+    mn[j] = hmm[2 * j];
+    mx[j] = hmm[2 * j + 1];
+  }
+  int bucket = ec.bucket;
+  if (!(eps0 > 0) || !std::isfinite((double)eps0)) {
+    // The reference divides by a zero epsilon here (N <= 1000 gives a zero
+    // sampled mean); any positive width keeps the join exact.
+    eps0 = host_fallback_eps<T>(mn, mx, n, K);
+    bucket = -1;
+  }
+  if (st) {
+    st->eps0 = (double)eps0;
+    st->eps_bucket = bucket;
+    st->avg_distance = hs->avg[0];
+  }
+
+  // 4. grid at eps0
+  DeviceGrid<T> grid;
+  build_grid<T>(w, cfg, n, d, di, mn, mx, eps0, &grid, s);
+  if (st) st->nonempty_cells = grid.C;
+  KNNSJ_CUDA(cudaEventRecord(ev[1], s));
+
+  // 5. retry loop
+  uint32_t* list[2] = {(uint32_t*)w.list0.get(n * 4), (uint32_t*)w.list1.get(n * 4)};
+  SearchLaunch<T> a;
+  a.grid = grid;
+  a.xs = xs;
+  a.n = n;
+  a.d = d;
+  a.K = K;
+  a.out_ids = d_ids;
+  a.out_d = d_dists;
+  a.fail_count = &sm->fail_count;
+  a.cand_count = &sm->cand;
+  a.work_counter = &sm->work_counter;
+  T r = eps0;
+  const double step = (double)eps0 * 0.5;
+  uint32_t nq = (uint32_t)n;
+  int iter = 0, regrids = 0, cur = 0;
+  uint64_t queries_run = 0;
+  const int max_iter = cfg.max_iterations > 0 ? cfg.max_iterations : 100000;
+  while (nq > 0) {
+    if (iter >= max_iter) throw StatusError{KNNSJ_ERR_NO_CONVERGENCE, "iteration cap reached"};
+    const double rows = ring_rows((double)r, (double)a.grid.geom.width, di);
+    const double allowed = std::max(std::pow(3.0, (double)(di - 1)), 64.0);
+    if (rows > allowed && (double)r > (double)a.grid.geom.width) {
+      // coarser grid at the current radius (like main.cu:333-356); the
+      // widened width keeps the ring at three cells per dimension
+      const T wnew = (T)((double)r * (1.0 + 1.0 / 32768.0));
+      build_grid<T>(w, cfg, n, d, di, mn, mx, wnew, &a.grid, s);
+      regrids++;
+    }
+    a.qlist = iter == 0 ? nullptr : list[cur];
+    a.nq = nq;
+    a.radius = r;
+    a.fail_list = list[cur ^ 1];
+    KNNSJ_CUDA(cudaMemsetAsync(&sm->fail_count, 0, 4, s));
+    launch_search<T>(a, w.sm_count, s);
+    uint32_t nfail = 0;
+    KNNSJ_CUDA(cudaMemcpyAsync(&nfail, &sm->fail_count, 4, cudaMemcpyDeviceToHost, s));
+    KNNSJ_CUDA(cudaStreamSynchronize(s));
+    queries_run += nq;
+    nq = nfail;
+    cur ^= 1;
+    iter++;
+    if (nq > 0) r = (T)((double)r + step);  // main.cu:336
+  }
+  KNNSJ_CUDA(cudaEventRecord(ev[2], s));
+  unsigned long long cand = 0;
+  KNNSJ_CUDA(cudaMemcpyAsync(&cand, &sm->cand, 8, cudaMemcpyDeviceToHost, s));
+  KNNSJ_CUDA(cudaStreamSynchronize(s));
+  if (st) {
+    st->iterations = iter;
+    st->regrids = regrids;
+    st->eps_final = (double)r;
+    st->candidates = cand;
+    st->queries_run = queries_run;
+    float a01 = 0, a12 = 0;
+    cudaEventElapsedTime(&a01, ev[0], ev[1]);
+    cudaEventElapsedTime(&a12, ev[1], ev[2]);
+    st->ms_prep = a01;
+    st->ms_search = a12;
+    st->ms_total = a01 + a12;
+  }
+}
+
+template void run_join<float>(Workspace&, const JoinConfig&, const float*, const float*, uint64_t, uint32_t,
+                              uint32_t, int32_t*, float*, knnsj_stats*, cudaStream_t);
+template void run_join<double>(Workspace&, const JoinConfig&, const double*, const double*, uint64_t,
+                               uint32_t, uint32_t, int32_t*, double*, knnsj_stats*, cudaStream_t);
+
+}  // namespace knnsj

@@ -1,0 +1,152 @@
+// knnsj_internal.h -- host-side declarations shared by the library's
+// translation units (kernel launchers, pipeline, host I/O).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cstdio>
+#include <cuda_runtime.h>
+
+#include "../../include/knnsj.h"
+#include "knnsj_device.cuh"
+
+namespace knnsj {
+
+// ---- error plumbing ------------------------------------------------------
+struct CudaError {
+  cudaError_t err;
+  const char* where;
+};
+
+#define KNNSJ_CUDA(call)                                                   \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess) throw ::knnsj::CudaError{e_, #call};            \
+  } while (0)
+
+struct StatusError {
+  knnsj_status st;
+  const char* what;
+};
+
+// ---- device buffers of one join (cached across calls, grow-only) --------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  void* get(size_t need);  // grows with cudaMalloc (contents not kept)
+  void release();
+};
+
+// Grid index on the device, in cell order.
+template <typename T>
+struct DeviceGrid {
+  GridGeom<T> geom;
+  const T* ps = nullptr;                  // SoA coords in cell order: d x n
+  const uint32_t* pid = nullptr;          // original id of each sorted position
+  const unsigned long long* ckeys = nullptr;  // sorted non-empty cell ids [C]
+  const uint32_t* coff = nullptr;         // first sorted position of each cell [C+1]
+  const uint32_t* dstart = nullptr;       // dense: first position of cell L [total+1]
+  unsigned long long C = 0;
+  int dense = 0;
+};
+
+// ---- kernel launchers (k_*.cu) -------------------------------------------
+template <typename T>
+void launch_transpose_reorder(const T* aos, T* soa, uint64_t n, uint32_t d, const uint32_t* d_perm,
+                              cudaStream_t s, uint32_t* d_nonfinite);
+template <typename T>
+void launch_minmax(const T* soa, uint64_t n, uint32_t di, T* d_minmax /*2*di*/, T* scratch /*1024*2*di*/,
+                   cudaStream_t s);
+
+struct EpsScratch {
+  double* partial = nullptr;            // [n_avg_threads]
+  unsigned long long* pcount = nullptr;  // [n_avg_threads]
+  double* avg_out = nullptr;            // [2]: avg, total count
+  uint32_t* hist = nullptr;             // [10000]
+};
+uint64_t eps_avg_threads(uint64_t n);
+uint32_t eps_sample_offset(uint64_t n);
+template <typename T>
+void launch_eps(const T* soa, uint64_t n, uint32_t d, const EpsScratch& sc, cudaStream_t s);
+
+struct GridScratch {
+  unsigned long long* keys[2] = {nullptr, nullptr};
+  uint32_t* vals[2] = {nullptr, nullptr};
+  uint32_t* hist = nullptr;   // radix tile histograms
+  uint32_t* scan_tmp = nullptr;
+  uint32_t* flags = nullptr;
+  size_t hist_elems = 0;
+  size_t scan_tmp_elems = 0;
+};
+size_t radix_hist_elems(uint64_t n);
+size_t scan_tmp_elems(size_t n);
+void scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, uint32_t* tmp, cudaStream_t s);
+
+template <typename T>
+void launch_cell_ids(const T* soa, uint64_t n, const GridGeom<T>& g, unsigned long long* keys,
+                     uint32_t* vals, cudaStream_t s);
+// Stable LSD radix sort of (key, value) by the low `bits` bits of key.
+// Returns the index (0/1) of the buffers holding the result.
+int radix_sort_pairs(GridScratch& sc, uint64_t n, int bits, cudaStream_t s);
+// Non-empty cell table from sorted keys; writes C to *d_C.
+void launch_compact_cells(const unsigned long long* skeys, uint64_t n, uint32_t* flags,
+                          uint32_t* pos, uint32_t* scan_tmp, unsigned long long* ckeys,
+                          uint32_t* coff, unsigned long long* d_C, cudaStream_t s);
+void launch_dense_table(const unsigned long long* ckeys, const uint32_t* coff,
+                        unsigned long long C, unsigned long long total_cells, uint32_t* dstart,
+                        cudaStream_t s);
+template <typename T>
+void launch_gather_sorted(const T* soa, uint64_t n, uint32_t d, const uint32_t* sorted_ids, T* ps,
+                          cudaStream_t s);
+
+// ---- range search with fused top-K --------------------------------------
+template <typename T>
+struct SearchLaunch {
+  DeviceGrid<T> grid;
+  const T* xs = nullptr;            // SoA coords in input order (failed queries)
+  uint64_t n = 0;
+  uint32_t d = 0;
+  uint32_t K = 0;
+  const uint32_t* qlist = nullptr;  // original ids; nullptr = all, in cell order
+  uint32_t nq = 0;
+  T radius = 0;                     // uniform radius (qradius == nullptr)
+  T* qradius = nullptr;             // per-query radius by original id
+  T step = 0;                       // radius growth written back on failure
+  int32_t* out_ids = nullptr;
+  T* out_d = nullptr;
+  uint32_t* fail_list = nullptr;
+  uint32_t* fail_count = nullptr;
+  unsigned long long* cand_count = nullptr;
+  uint32_t* work_counter = nullptr;
+};
+template <typename T>
+void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s);
+int search_buffer_capacity(uint32_t K);
+
+// ---- per-device workspace --------------------------------------------------
+struct Workspace {
+  DevBuf in, ids, dists;                 // staging for host-pointer calls
+  DevBuf xs, ps, pid;                    // input-order columns, cell-order columns, ids
+  DevBuf keys0, keys1, vals0, vals1, hist, scan_tmp, flags, pos;  // grid build
+  DevBuf ckeys, coff, dstart;            // cell tables
+  DevBuf list0, list1, small, eps_partial, eps_pcount, perm, minmax_part, qradius;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  int sm_count = 0;
+  void* h_pinned = nullptr;
+  size_t h_pinned_bytes = 0;
+  void ensure_stream();
+  void* pinned(size_t need);
+  void pinned_release();
+  void release_all();
+};
+Workspace& workspace(int device);
+
+struct JoinConfig;
+// Full join of n x d row-major data already on the device.  h_aos (optional)
+// is the same data on the host, used for the dimension-order sample.
+template <typename T>
+void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
+              uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s);
+
+}  // namespace knnsj
