@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Benchmark of the exact kNN self-join on GB300.
+
+Workload (one "step"): the full self-join of the 25M-point 2-D float32
+sky-like dataset at k=64, BETA=0.025 (the configuration the reference's
+headline figure is quoted on, README.md:34-37, with a seeded synthetic
+stand-in for the Gaia DR2 file) -- reorder, eps0, grid build, and every
+search pass -- with the points resident in HBM and the N x (k+1) result
+table left in HBM.  value = queries/s over all ranks.  e2e = the same join
+through the host API (knnsj_selfjoin) from pinned host memory, host->device
+input copy and device->host result copy inside the timed region.
+
+The reference arm (--impl reference) times the CPU restatement of the
+reference's algorithm (oracle/) on the host cores, on a bounded sample.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "sky2d_25m"
+METRIC = "exact KNN queries/s on 1 GB300: learned-radius vs plain BETA; HBM roofline %"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self, world: int, backend: str):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64, device="cuda" if self.pg.get_backend() == "nccl" else "cpu")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.idx = device_index
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            j = json.load(f)
+        return {"hbm_gbs": float(j["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic(workload: str):
+    """DRAM traffic per search launch from the committed ncu summary, scaled to
+    this workload when the capture was a smaller case of the same kernel."""
+    p = os.path.join(ROOT, "profiles", "search_kernel_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        j = json.load(f)
+    return j.get(workload)
+
+
+def cpu_baseline(x, k: int, beta: float, di: int, n_sample: int, seed: int = 0) -> dict:
+    """The oracle (CPU restatement of the reference pipeline) on all host
+    cores: full preprocessing of all points plus the search of a seeded query
+    subsample, extrapolated linearly to all N queries."""
+    import numpy as np
+
+    import oracle
+    n = x.shape[0]
+    q = np.sort(np.random.default_rng(seed).choice(n, n_sample, replace=False)).astype(np.uint32)
+    threads = oracle.max_threads()
+    rc, _, _, st = oracle.join(x, k, di=di, beta=beta, queries=q)
+    assert rc == 0, rc
+    # preprocessing and the grid rebuilds of each radius growth cost the same
+    # for any number of queries; only the search passes scale with them
+    t_full = st.seconds_prep + st.seconds_regrid + st.seconds_search * n / n_sample
+    return {"value": n / t_full, "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": (f"oracle/ (CPU restatement of the reference pipeline, OpenMP, {threads} threads): "
+                       f"reorder + eps0 + grid on all {n} points ({st.seconds_prep:.2f} s), "
+                       f"{st.reindexes} grid rebuilds ({st.seconds_regrid:.2f} s) and the search passes of a "
+                       f"seeded {n_sample}-query subsample ({st.seconds_search:.2f} s, {st.iterations} passes), "
+                       f"search time scaled by N/{n_sample}"),
+            "ms_per_join_extrapolated": t_full * 1e3}
+
+
+def make_workload():
+    from hybrid_k_nearest_neighbor_self_join_gb300 import datasets
+    gen, k, beta, di = datasets.CONFIGS[WORKLOAD]
+    return gen(), k, beta, di
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    x, k, beta, di = make_workload()
+    n = x.shape[0]
+    res = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(x, k, beta, di, args.cpu_sample, seed=i)
+        if i >= args.warmup:
+            res.append(r)
+    vals = [r["value"] for r in res]
+    v = statistics.median(vals)
+    ms = statistics.median([r["ms_per_join_extrapolated"] for r in res])
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_points": n, "d": 2, "k": k, "beta": beta, "num_indexed_dims": di},
+        "cpu_baseline": {"value": v, "unit": "queries/s", "cores": res[0]["cores"], "kind": "port",
+                         "sample": res[0]["sample"]},
+        "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    import hybrid_k_nearest_neighbor_self_join_gb300 as kj
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = Dist(world, "nccl")
+    x, k, beta, di = make_workload()
+    n, d = x.shape
+    K = k + 1
+    # ---- device-resident join -------------------------------------------
+    tx = torch.from_numpy(x).cuda()
+    tids = torch.empty((n, K), dtype=torch.int32, device="cuda")
+    td = torch.empty((n, K), dtype=torch.float32, device="cuda")
+
+    def step():
+        return kj.selfjoin_device(tx.data_ptr(), np.float32, n, d, k, tids.data_ptr(), td.data_ptr(),
+                                  num_indexed_dims=di, beta=beta)
+
+    st = None
+    for _ in range(args.warmup):
+        st = step()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    launches = 0
+    kernel_ms, alg_bytes, iters = [], [], []
+    for _ in range(args.steps):
+        st = step()
+        launches += st["kernel_launches"]
+        kernel_ms.append(st["ms_search_kernels"])
+        alg_bytes.append(st["search_alg_bytes"])
+        iters.append(st["iterations"])
+    e1.record()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    t_ms = dist.max(e0.elapsed_time(e1))
+    ms_per_step = t_ms / args.steps
+    value = n * world * args.steps / (t_ms / 1e3)
+
+    # ---- end to end through the host API, pinned buffers ------------------
+    hx = torch.from_numpy(x).pin_memory()
+    hids = torch.empty((n, K), dtype=torch.int32).pin_memory()
+    hd = torch.empty((n, K), dtype=torch.float32).pin_memory()
+    xs_np, ids_np, d_np = hx.numpy(), hids.numpy(), hd.numpy()
+    kj.selfjoin(xs_np, k, num_indexed_dims=di, beta=beta, out_ids=ids_np, out_dists=d_np)
+    torch.cuda.synchronize()
+    dist.barrier()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    e2.record()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        kj.selfjoin(xs_np, k, num_indexed_dims=di, beta=beta, out_ids=ids_np, out_dists=d_np)
+    e3.record()
+    torch.cuda.synchronize()
+    t_e2e = dist.max(e2.elapsed_time(e3))
+    e2e_value = n * world * e2e_steps / (t_e2e / 1e3)
+
+    # ---- roofline of the dominant kernel (the search) ----------------------
+    pk = peaks()
+    kms = statistics.median(kernel_ms)
+    ab = statistics.median(alg_bytes)
+    achieved = ab / (kms / 1e3) / 1e9
+    tr = ncu_traffic(WORKLOAD)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "traffic": tr["dram_bytes_per_join"] if tr else None,
+                "kernel": "search_kernel<float,2>", "kernel_ms_per_step": kms,
+                "alg_bytes_per_step": ab, "peak_source": pk["source"] + " hbm_gbs (MEASURED_PEAKS.json)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_points": n, "d": d, "k": k, "beta": beta, "num_indexed_dims": di,
+                   "radius": "plain BETA schedule", "parallelism": f"replicas x{world}",
+                   "l2": "inputs (200 MB) and outputs (13 GB) exceed the 129 MB L2; no flush"},
+        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(n * d * 4),
+                "d2h_bytes_per_step": int(n * K * 8)},
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "clocks": clk,
+        "search_iterations": statistics.median(iters),
+        "stats_last_step": {kk: st[kk] for kk in ("eps0", "iterations", "regrids", "candidates", "ms_prep",
+                                                  "ms_search", "ms_search_kernels", "nonempty_cells")},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(x, k, beta, di, args.cpu_sample)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+def run_profile_case(which: str):
+    """One device-resident join for profiler captures.  'full' is the bench
+    workload; 'slice' is its longitude slice x < 57.6 deg (about 4M points,
+    the same densities), small enough for multi-pass ncu captures."""
+    import numpy as np
+    import torch
+
+    import hybrid_k_nearest_neighbor_self_join_gb300 as kj
+    x, k, beta, di = make_workload()
+    if which == "slice":
+        x = np.ascontiguousarray(x[x[:, 0] < 57.6])
+    n, d = x.shape
+    tx = torch.from_numpy(x).cuda()
+    tids = torch.empty((n, k + 1), dtype=torch.int32, device="cuda")
+    td = torch.empty((n, k + 1), dtype=torch.float32, device="cuda")
+    st = kj.selfjoin_device(tx.data_ptr(), np.float32, n, d, k, tids.data_ptr(), td.data_ptr(),
+                            num_indexed_dims=di, beta=beta)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": which, "n": n, **{kk: st[kk] for kk in (
+        "eps0", "iterations", "regrids", "candidates", "queries_run", "ms_prep", "ms_search", "ms_search_kernels",
+        "search_alg_bytes", "kernel_launches")}}), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=20000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", choices=["full", "slice"], default=None,
+                    help="run one join for a profiler capture and exit")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warning: fewer than 3 warm-up steps")
+    if args.impl == "reference":
+        return run_reference(args)
+    import __graft_entry__
+    __graft_entry__.build_library()
+    if args.profile_case:
+        return run_profile_case(args.profile_case)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

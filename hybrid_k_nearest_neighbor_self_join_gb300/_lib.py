@@ -78,6 +78,10 @@ class Stats(ctypes.Structure):
         ("ms_search", ctypes.c_double),
         ("ms_transfer", ctypes.c_double),
         ("perm", ctypes.c_uint32 * 64),
+        ("kernel_launches", ctypes.c_uint64),
+        ("ms_search_kernels", ctypes.c_double),
+        ("search_alg_bytes", ctypes.c_double),
+        ("search_alg_flops", ctypes.c_double),
         ("reserved", ctypes.c_double * 8),
     ]
 

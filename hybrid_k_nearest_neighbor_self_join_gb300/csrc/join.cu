@@ -31,6 +31,8 @@
 
 namespace knnsj {
 
+unsigned long long g_launches = 0;
+
 void* DevBuf::get(size_t need) {
   if (need == 0) need = 16;
   if (need > bytes) {
@@ -205,6 +207,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   const uint32_t K = k + 1;
   const uint32_t di = cfg.num_indexed_dims;
   cudaEvent_t* ev = w.ev;
+  g_launches = 0;
   KNNSJ_CUDA(cudaEventRecord(ev[0], s));
 
   // 1. dimension order
@@ -296,6 +299,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   uint32_t nq = (uint32_t)n;
   int iter = 0, regrids = 0, cur = 0;
   uint64_t queries_run = 0;
+  double kernel_ms = 0.0, alg_bytes = 0.0;
   const int max_iter = cfg.max_iterations > 0 ? cfg.max_iterations : 100000;
   while (nq > 0) {
     if (iter >= max_iter) throw StatusError{KNNSJ_ERR_NO_CONVERGENCE, "iteration cap reached"};
@@ -313,10 +317,18 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     a.radius = r;
     a.fail_list = list[cur ^ 1];
     KNNSJ_CUDA(cudaMemsetAsync(&sm->fail_count, 0, 4, s));
+    KNNSJ_CUDA(cudaEventRecord(ev[4], s));
     launch_search<T>(a, w.sm_count, s);
+    KNNSJ_CUDA(cudaEventRecord(ev[5], s));
     uint32_t nfail = 0;
     KNNSJ_CUDA(cudaMemcpyAsync(&nfail, &sm->fail_count, 4, cudaMemcpyDeviceToHost, s));
     KNNSJ_CUDA(cudaStreamSynchronize(s));
+    float kms = 0.f;
+    KNNSJ_CUDA(cudaEventElapsedTime(&kms, ev[4], ev[5]));
+    kernel_ms += kms;
+    // candidate columns read once, query rows read, accepted rows written
+    alg_bytes += (double)n * d * sizeof(T) + (double)nq * d * sizeof(T) +
+                 (double)(nq - nfail) * K * (4.0 + sizeof(T));
     queries_run += nq;
     nq = nfail;
     cur ^= 1;
@@ -333,6 +345,10 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     st->eps_final = (double)r;
     st->candidates = cand;
     st->queries_run = queries_run;
+    st->kernel_launches = g_launches;
+    st->ms_search_kernels = kernel_ms;
+    st->search_alg_bytes = alg_bytes;
+    st->search_alg_flops = 3.0 * d * (double)cand;
     float a01 = 0, a12 = 0;
     cudaEventElapsedTime(&a01, ev[0], ev[1]);
     cudaEventElapsedTime(&a12, ev[1], ev[2]);

@@ -162,16 +162,16 @@ void launch_eps(const T* soa, uint64_t n, uint32_t d, const EpsScratch& sc, cuda
   if (nthr > 0) {
     eps_avg_kernel<T><<<(unsigned)(nthr / EPS_BLOCK), EPS_BLOCK, 0, s>>>(soa, n, d, nthr, sc.partial,
                                                                       sc.pcount);
-    KNNSJ_CUDA(cudaGetLastError());
+    KNNSJ_CHECK_LAUNCH();
   }
   eps_avg_final_kernel<<<1, 32, 0, s>>>(sc.partial, sc.pcount, nthr, sc.avg_out);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
   KNNSJ_CUDA(cudaMemsetAsync(sc.hist, 0, NBUCKETS * sizeof(uint32_t), s));
   const uint32_t offset = eps_sample_offset(n);
   const uint32_t blocks2 = (uint32_t)n / offset;  // GPU.cu:3440 (integer division)
   if (blocks2 > 0) {
     eps_hist_kernel<T><<<blocks2, EPS_BLOCK, 0, s>>>(soa, n, d, offset, sc.avg_out, sc.hist);
-    KNNSJ_CUDA(cudaGetLastError());
+    KNNSJ_CHECK_LAUNCH();
   }
 }
 

@@ -288,18 +288,18 @@ void scan_exclusive_u32(const uint32_t* in, uint32_t* out, size_t n, uint32_t* t
   if (n == 0) return;
   const size_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
   scan_reduce_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, tmp);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
   scan_sums_kernel<<<1, SCAN_THREADS, 0, s>>>(tmp, nb);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
   scan_apply_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, tmp, out);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
 }
 
 template <typename T>
 void launch_cell_ids(const T* soa, uint64_t n, const GridGeom<T>& g, unsigned long long* keys,
                      uint32_t* vals, cudaStream_t s) {
   cell_id_kernel<T><<<grid_blocks(n), 256, 0, s>>>(soa, n, g, keys, vals);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
 }
 
 int radix_sort_pairs(GridScratch& sc, uint64_t n, int bits, cudaStream_t s) {
@@ -308,11 +308,11 @@ int radix_sort_pairs(GridScratch& sc, uint64_t n, int bits, cudaStream_t s) {
   const size_t nh = (size_t)256 * ntiles;
   for (int shift = 0; shift < bits; shift += 8) {
     radix_hist_kernel<<<ntiles, RS_THREADS, 0, s>>>(sc.keys[cur], n, shift, ntiles, sc.hist);
-    KNNSJ_CUDA(cudaGetLastError());
+    KNNSJ_CHECK_LAUNCH();
     scan_exclusive_u32(sc.hist, sc.hist, nh, sc.scan_tmp, s);
     radix_scatter_kernel<<<ntiles, RS_THREADS, 0, s>>>(sc.keys[cur], sc.vals[cur], sc.keys[cur ^ 1],
                                                        sc.vals[cur ^ 1], n, shift, ntiles, sc.hist);
-    KNNSJ_CUDA(cudaGetLastError());
+    KNNSJ_CHECK_LAUNCH();
     cur ^= 1;
   }
   return cur;
@@ -322,25 +322,25 @@ void launch_compact_cells(const unsigned long long* skeys, uint64_t n, uint32_t*
                           uint32_t* scan_tmp, unsigned long long* ckeys, uint32_t* coff,
                           unsigned long long* d_C, cudaStream_t s) {
   cell_flags_kernel<<<grid_blocks(n), 256, 0, s>>>(skeys, n, flags);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
   scan_exclusive_u32(flags, pos, n, scan_tmp, s);
   cell_compact_kernel<<<grid_blocks(n), 256, 0, s>>>(skeys, n, pos, ckeys, coff);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
   cell_count_kernel<<<1, 32, 0, s>>>(skeys, n, pos, coff, d_C);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
 }
 
 void launch_dense_table(const unsigned long long* ckeys, const uint32_t* coff, unsigned long long C,
                         unsigned long long total_cells, uint32_t* dstart, cudaStream_t s) {
   dense_table_kernel<<<grid_blocks(total_cells + 1), 256, 0, s>>>(ckeys, coff, C, total_cells, dstart);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
 }
 
 template <typename T>
 void launch_gather_sorted(const T* soa, uint64_t n, uint32_t d, const uint32_t* sorted_ids, T* ps,
                           cudaStream_t s) {
   gather_sorted_kernel<T><<<grid_blocks(n), 256, 0, s>>>(soa, n, d, sorted_ids, ps);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
 }
 
 template void launch_cell_ids<float>(const float*, uint64_t, const GridGeom<float>&, unsigned long long*,

@@ -95,7 +95,7 @@ void launch_transpose_reorder(const T* aos, T* soa, uint64_t n, uint32_t d, cons
   uint64_t blocks = (n + 255) / 256;
   if (blocks > 152ull * 32) blocks = 152ull * 32;
   transpose_reorder_kernel<T><<<(unsigned)blocks, 256, 0, s>>>(aos, soa, n, d, d_perm, d_nonfinite);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
 }
 
 template <typename T>
@@ -104,9 +104,9 @@ void launch_minmax(const T* soa, uint64_t n, uint32_t di, T* d_minmax, T* scratc
   if (blocks > MINMAX_BLOCKS) blocks = MINMAX_BLOCKS;
   if (blocks < 1) blocks = 1;
   minmax_kernel<T><<<blocks, 256, 0, s>>>(soa, n, di, scratch);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
   minmax_final_kernel<T><<<1, 32, 0, s>>>(scratch, blocks, di, d_minmax);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
 }
 
 template void launch_transpose_reorder<float>(const float*, float*, uint64_t, uint32_t, const uint32_t*,

@@ -262,7 +262,7 @@ void launch_one(const SearchParams<T>& prm, int sm_count, cudaStream_t s) {
   if (need_blocks < blocks) blocks = need_blocks;
   if (blocks < 1) blocks = 1;
   kern<<<(unsigned)blocks, wpb * 32, smem, s>>>(prm);
-  KNNSJ_CUDA(cudaGetLastError());
+  KNNSJ_CHECK_LAUNCH();
 }
 
 }  // namespace

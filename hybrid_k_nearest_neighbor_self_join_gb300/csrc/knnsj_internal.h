@@ -29,6 +29,14 @@ struct StatusError {
   const char* what;
 };
 
+// Kernel launches since the last reset (reported in knnsj_stats).
+extern unsigned long long g_launches;
+#define KNNSJ_CHECK_LAUNCH()                 \
+  do {                                       \
+    KNNSJ_CUDA(cudaGetLastError());          \
+    ++::knnsj::g_launches;                   \
+  } while (0)
+
 // ---- device buffers of one join (cached across calls, grow-only) --------
 struct DevBuf {
   void* p = nullptr;
@@ -131,7 +139,7 @@ struct Workspace {
   DevBuf ckeys, coff, dstart;            // cell tables
   DevBuf list0, list1, small, eps_partial, eps_pcount, perm, minmax_part, qradius;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   int sm_count = 0;
   void* h_pinned = nullptr;
   size_t h_pinned_bytes = 0;

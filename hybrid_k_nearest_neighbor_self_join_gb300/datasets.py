@@ -40,8 +40,7 @@ def sky_like(n: int = 25_000_000, seed: int = 1, n_clumps: int = 200, clump_frac
     cl = np.repeat(centres, per, axis=0) + rng.normal(0.0, clump_sd, (n_cl, 2))
     cl[:, 1] = np.clip(cl[:, 1], -90.0, 90.0)
     pts = np.concatenate([base, cl]).astype(dtype)
-    rng.shuffle(pts, axis=0)
-    return np.ascontiguousarray(pts)
+    return np.ascontiguousarray(pts[rng.permutation(n)])
 
 
 def gmm(n: int, d: int, n_comp: int, uniform_frac: float, seed: int, sd_lo: float = 0.005,
@@ -57,8 +56,7 @@ def gmm(n: int, d: int, n_comp: int, uniform_frac: float, seed: int, sd_lo: floa
     pts = np.empty((n, d), dtype=dtype)
     pts[:n_g] = (centres[lab] + rng.standard_normal((n_g, d)) * sds[lab]).astype(dtype)
     pts[n_g:] = rng.random((n_u, d)).astype(dtype)
-    rng.shuffle(pts, axis=0)
-    return pts
+    return np.ascontiguousarray(pts[rng.permutation(n)])
 
 
 def gmm6d(n: int = 10_000_000, seed: int = 2) -> np.ndarray:

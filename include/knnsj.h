@@ -93,6 +93,11 @@ typedef struct {
   double ms_search;          /* all search passes */
   double ms_transfer;        /* host<->device copies (host-pointer calls) */
   uint32_t perm[64];         /* dimension order used (first min(d,64)) */
+  uint64_t kernel_launches;  /* CUDA kernels launched by the join */
+  double ms_search_kernels;  /* device time of the search kernel launches only */
+  double search_alg_bytes;   /* algorithmic bytes of all search passes:
+                                sum over passes of N*d*s + Q*d*s + accepted*(k+1)*(4+s) */
+  double search_alg_flops;   /* 3*d per scanned candidate */
   double reserved[8];
 } knnsj_stats;
 

@@ -33,6 +33,9 @@ class OrcStats(ctypes.Structure):
         ("eps_offset", ctypes.c_uint32),
         ("eps_sample_blocks", ctypes.c_uint32),
         ("perm", ctypes.c_uint32 * 64),
+        ("seconds_prep", ctypes.c_double),
+        ("seconds_regrid", ctypes.c_double),
+        ("seconds_search", ctypes.c_double),
     ]
 
 

@@ -38,6 +38,7 @@
 #include <limits>
 #include <vector>
 #include <omp.h>
+#include <parallel/algorithm>
 
 namespace {
 
@@ -313,8 +314,10 @@ void build_grid(const T* X, uint64_t n, uint32_t d, Grid<T>* g, int nthreads) {
 #pragma omp parallel for num_threads(nthreads)
   for (int64_t i = 0; i < (int64_t)n; i++) kv[i] = {point_cell(X + (uint64_t)i * d, *g), (uint32_t)i};
   // stable by construction: the pair sort orders equal cells by point id,
-  // as the reference's radix sort_by_key does (GPU.cu:3959).
-  std::sort(kv.begin(), kv.end());
+  // as the reference's radix sort_by_key does (GPU.cu:3959).  Parallel as
+  // the reference's host grid sort (par_sort.cpp:7-10); pairs are unique, so
+  // the order does not depend on the sorting algorithm.
+  __gnu_parallel::sort(kv.begin(), kv.end());
   g->lookup.resize(n);
   g->cellKeys.clear();
   g->indexmin.clear();
@@ -430,6 +433,9 @@ typedef struct {
   uint32_t eps_offset;
   uint32_t eps_sample_blocks;
   uint32_t perm[64];        // dimension order after ReorderByDimension
+  double seconds_prep;      // reorder + epsilon + first grid
+  double seconds_regrid;    // grid rebuilds on epsilon growth
+  double seconds_search;    // search passes
 } orc_stats;
 }
 
@@ -453,6 +459,7 @@ int join_impl(const T* data, uint64_t n, uint32_t d, uint32_t k, int32_t di, dou
   if ((uint32_t)di > d) return 1;
   nthreads = clamp_threads(nthreads);
   std::memset(s, 0, sizeof(*s));
+  const double t_start = omp_get_wtime();
   std::vector<uint32_t> perm(d);
   for (uint32_t j = 0; j < d; j++) perm[j] = j;
   if (reorder) reorder_permutation<T>(data, n, d, perm.data(), (T*)nullptr);
@@ -480,6 +487,7 @@ int join_impl(const T* data, uint64_t n, uint32_t d, uint32_t k, int32_t di, dou
   Grid<T> g;
   grid_dimensions<T>(X.data(), n, d, (uint32_t)di, eps, &g);
   build_grid<T>(X.data(), n, d, &g, nthreads);
+  s->seconds_prep = omp_get_wtime() - t_start;
   double failPrev = 0.0;
   int iter = 0;
   uint64_t scanned_total = 0;
@@ -487,11 +495,13 @@ int join_impl(const T* data, uint64_t n, uint32_t d, uint32_t k, int32_t di, dou
     if (max_iterations > 0 && iter >= max_iterations) return 6;
     bool repeat_same = false;
     if (iter != 0 && failPrev > 0.25) {
+      const double t0 = omp_get_wtime();
       eps = (T)((double)eps + (double)eps0 * 0.5);  // main.cu:336
       if (eps == 0) return 10;                       // main.cu:338-342
       grid_dimensions<T>(X.data(), n, d, (uint32_t)di, eps, &g);
       build_grid<T>(X.data(), n, d, &g, nthreads);
       s->reindexes++;
+      s->seconds_regrid += omp_get_wtime() - t0;
     } else if (iter != 0) {
       // main.cu:330: at most 25% failed, so the failed queries run again at
       // the same epsilon.  That pass is deterministic and fails them all, so
@@ -501,6 +511,7 @@ int join_impl(const T* data, uint64_t n, uint32_t d, uint32_t k, int32_t di, dou
     const uint64_t nactive = active.size();
     std::vector<uint8_t> ok(nactive, 0);
     if (!repeat_same) {
+      const double t0 = omp_get_wtime();
       uint64_t sc = 0;
 #pragma omp parallel num_threads(nthreads) reduction(+ : sc)
       {
@@ -513,6 +524,7 @@ int join_impl(const T* data, uint64_t n, uint32_t d, uint32_t k, int32_t di, dou
         }
       }
       scanned_total += sc;
+      s->seconds_search += omp_get_wtime() - t0;
     }
     std::vector<uint32_t> failed;
     for (uint64_t a = 0; a < nactive; a++)
