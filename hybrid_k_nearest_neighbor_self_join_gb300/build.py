@@ -43,7 +43,7 @@ def _nvcc() -> str:
 
 
 def _knob_defines() -> list[str]:
-    defs = []
+    defs = os.environ.get("KNNSJ_NVCC_EXTRA", "").split()
     for env, macro in (("KNNSJ_GPUNUMDIM", "GPUNUMDIM"), ("KNNSJ_NUMINDEXEDDIM", "NUMINDEXEDDIM"),
                        ("KNNSJ_BETA_BUILD", "BETA")):
         v = os.environ.get(env)

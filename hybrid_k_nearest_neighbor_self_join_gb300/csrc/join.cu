@@ -68,7 +68,7 @@ Workspace& workspace(int device) {
 void Workspace::release_all() {
   DevBuf* bufs[] = {&in, &ids, &dists, &xs, &ps, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
                     &scan_tmp, &flags, &pos, &ckeys, &coff, &dstart, &list0, &list1, &small,
-                    &eps_partial, &eps_pcount, &perm, &minmax_part, &qradius};
+                    &eps_partial, &eps_sample, &perm, &minmax_part, &qradius};
   for (DevBuf* b : bufs) b->release();
   if (stream) cudaStreamDestroy(stream);
   stream = nullptr;
@@ -111,6 +111,8 @@ struct SmallDev {  // layout of Workspace::small
   unsigned long long cand;
   double avg[2];
   uint32_t hist[10000];
+  double csum;
+  double cpart[1024];
 };
 
 template <typename T>
@@ -236,26 +238,46 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   KNNSJ_CUDA(cudaMemcpyAsync(d_perm, perm.data(), d * 4, cudaMemcpyHostToDevice, s));
   T* xs = (T*)w.xs.get(n * d * sizeof(T));
   launch_transpose_reorder<T>(d_aos, xs, n, d, d_perm, s, &sm->nonfinite);
-  T* mm_part = (T*)w.minmax_part.get(1024 * 2 * di * sizeof(T) + 2 * di * sizeof(T));
-  T* d_minmax = mm_part + 1024 * 2 * di;
-  launch_minmax<T>(xs, n, di, d_minmax, mm_part, s);
+  T* mm_part = (T*)w.minmax_part.get(1024 * 2 * d * sizeof(T) + 2 * d * sizeof(T));
+  T* d_minmax = mm_part + 1024 * 2 * d;
+  launch_minmax<T>(xs, n, d, d_minmax, mm_part, s);
 
   // 3. eps0 (GPU.cu:3088-3566)
   EpsScratch es;
   const uint64_t nthr = eps_avg_threads(n);
-  es.partial = (double*)w.eps_partial.get(std::max<uint64_t>(nthr, 1) * 8);
-  es.pcount = (unsigned long long*)w.eps_pcount.get(std::max<uint64_t>(nthr, 1) * 8);
+  es.partial = (double*)w.eps_partial.get(std::max<uint64_t>(nthr * eps_avg_chunks(n), 1) * 8);
+  es.sample_sum = (double*)w.eps_sample.get(std::max<uint64_t>(nthr, 1) * 8);
   es.avg_out = sm->avg;
   es.hist = sm->hist;
-  launch_eps<T>(xs, n, d, es, s);
-  std::vector<uint8_t> hsmall(sizeof(SmallDev));
-  std::vector<T> hmm(2 * di);
-  KNNSJ_CUDA(cudaMemcpyAsync(hmm.data(), d_minmax, 2 * di * sizeof(T), cudaMemcpyDeviceToHost, s));
-  KNNSJ_CUDA(cudaMemcpyAsync(hsmall.data(), sm, sizeof(SmallDev), cudaMemcpyDeviceToHost, s));
+  launch_eps_avg<T>(xs, n, d, es, s);
+  KNNSJ_CUDA(cudaMemsetAsync(sm->hist, 0, sizeof(sm->hist), s));
+  struct Head {
+    uint32_t nonfinite, fail_count, work_counter, pad;
+    unsigned long long C, cand;
+    double avg[2];
+  } head;
+  std::vector<T> hmm(2 * d);
+  KNNSJ_CUDA(cudaMemcpyAsync(hmm.data(), d_minmax, 2 * d * sizeof(T), cudaMemcpyDeviceToHost, s));
+  KNNSJ_CUDA(cudaMemcpyAsync(&head, sm, sizeof(head), cudaMemcpyDeviceToHost, s));
   KNNSJ_CUDA(cudaStreamSynchronize(s));
-  const SmallDev* hs = (const SmallDev*)hsmall.data();
-  if (hs->nonfinite) throw StatusError{KNNSJ_ERR_NONFINITE_INPUT, "NaN or infinite coordinate"};
-  const EpsChoice ec = choose_eps(hs->hist, hs->avg[0], n, k, cfg.beta);
+  if (head.nonfinite) throw StatusError{KNNSJ_ERR_NONFINITE_INPUT, "NaN or infinite coordinate"};
+  // float bracket error from rounding double coordinates to float
+  double max_abs = 0.0;
+  for (uint32_t j = 0; j < 2 * d; j++) max_abs = std::max(max_abs, std::fabs((double)hmm[j]));
+  const double abs_err = sizeof(T) == 8 ? std::sqrt((double)d) * std::ldexp(max_abs, -22) : 0.0;
+  // buckets [0, 256) first; the rest only if the crossing lies beyond
+  std::vector<uint32_t> hh(10000, 0);
+  const uint32_t first_range = 256;
+  launch_eps_hist<T>(xs, n, d, es, 0, first_range, abs_err, s);
+  KNNSJ_CUDA(cudaMemcpyAsync(hh.data(), sm->hist, first_range * 4, cudaMemcpyDeviceToHost, s));
+  KNNSJ_CUDA(cudaStreamSynchronize(s));
+  EpsChoice ec = choose_eps(hh.data(), first_range, head.avg[0], n, k, cfg.beta);
+  if (!ec.complete) {
+    launch_eps_hist<T>(xs, n, d, es, first_range, 10000, abs_err, s);
+    KNNSJ_CUDA(cudaMemcpyAsync(hh.data(), sm->hist, 10000 * 4, cudaMemcpyDeviceToHost, s));
+    KNNSJ_CUDA(cudaStreamSynchronize(s));
+    ec = choose_eps(hh.data(), 10000, head.avg[0], n, k, cfg.beta);
+  }
   T eps0 = (T)ec.eps;
   std::vector<T> mn(di), mx(di);
   for (uint32_t j = 0; j < di; j++) {
@@ -272,7 +294,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   if (st) {
     st->eps0 = (double)eps0;
     st->eps_bucket = bucket;
-    st->avg_distance = hs->avg[0];
+    st->avg_distance = head.avg[0];
   }
 
   // 4. grid at eps0
@@ -357,6 +379,18 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     st->ms_total = a01 + a12;
   }
 }
+
+template <typename T>
+double device_checksum(Workspace& w, const T* d_vals, uint64_t count, cudaStream_t s) {
+  SmallDev* sm = (SmallDev*)w.small.get(sizeof(SmallDev));
+  launch_checksum<T>(d_vals, count, sm->cpart, &sm->csum, s);
+  double v = 0.0;
+  KNNSJ_CUDA(cudaMemcpyAsync(&v, &sm->csum, sizeof(v), cudaMemcpyDeviceToHost, s));
+  KNNSJ_CUDA(cudaStreamSynchronize(s));
+  return v;
+}
+template double device_checksum<float>(Workspace&, const float*, uint64_t, cudaStream_t);
+template double device_checksum<double>(Workspace&, const double*, uint64_t, cudaStream_t);
 
 template void run_join<float>(Workspace&, const JoinConfig&, const float*, const float*, uint64_t, uint32_t,
                               uint32_t, int32_t*, float*, knnsj_stats*, cudaStream_t);

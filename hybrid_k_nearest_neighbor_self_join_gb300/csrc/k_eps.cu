@@ -2,23 +2,27 @@
 //
 // Restates sampleNeighborsBruteForce (GPU.cu:3088-3566) and its kernels:
 //   * kernelEstimateAvgDistBruteForce (kernel.cu:343-381): sample thread g
-//     takes point 1000*g and sums its distances to points t, t+1000, ...
-//     (t = g mod 256) in double.  The reference adds every distance to one
-//     double with atomicAdd, so its mean varies in the last bits from run to
-//     run; here each thread sums in loop order and one thread then adds the
-//     per-thread sums in thread order, a fixed order the oracle repeats.
+//     takes point 1000*g and sums, in double, its distances to points
+//     t, t+1000, ... (t = g mod 256).  The reference adds every distance to
+//     one double with atomicAdd, so its mean varies in the last bits from run
+//     to run.  Here the order is fixed: sample g's distances are summed in
+//     chunks of EPS_CHUNK consecutive terms, the chunk sums in chunk order,
+//     then the per-sample sums in sample order -- the order the oracle uses.
 //   * kernelKDistBruteForce (kernel.cu:450-523): block b takes point
 //     b*offset and bins its distances below the mean to every 8th block of
 //     256 points into 10 000 buckets of width mean/10000, 8 counts per hit.
 //     Reads past N (the reference leaves i+threadIdx.x unchecked,
 //     kernel.cu:486-492) are skipped and a bucket index that rounds up to
 //     10000 is dropped.
-// The host then picks eps0 from the cumulative histogram (GPU.cu:3480-3527).
+// eps0 depends only on the cumulative histogram up to the first bucket whose
+// neighbours per sampled point exceed k + (100k - k) * BETA (GPU.cu:3480-
+// 3527), so the histogram is built in two bucket ranges: [0, 256) first and
+// the rest only when the crossing is not in the first range.
 //
-// For float data each histogram distance is first bracketed in float: when
-// the bracket decides the bucket (and the below-mean test) unambiguously, the
-// double sqrt and division of the reference are skipped; otherwise they are
-// computed exactly as the reference does.  Either way the bucket equals the
+// Each histogram distance is first bracketed with float arithmetic and a
+// rigorous error bound; when the bracket settles the bucket (and the
+// below-mean test) the double sqrt and division are skipped, otherwise they
+// are computed exactly as the reference does.  The bucket is always the
 // reference's double-precision bucket.
 
 #include "knnsj_internal.h"
@@ -29,6 +33,7 @@ namespace {
 
 constexpr int EPS_BLOCK = 256;
 constexpr uint32_t NBUCKETS = 10000;
+constexpr uint32_t EPS_CHUNK = 256;
 
 // One squared-distance term as the reference's double accumulator receives
 // it: a float product widened (no contraction across the type change) or a
@@ -42,42 +47,63 @@ __device__ __forceinline__ double eps_term(double acc, double a, double b) {
   return __fma_rn(df, df, acc);
 }
 
-template <typename T>
-__global__ void eps_avg_kernel(const T* __restrict__ soa, uint64_t n, uint32_t d, uint64_t nthr,
-                               double* __restrict__ partial, unsigned long long* __restrict__ pcount) {
-  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= nthr) return;
-  const uint64_t tid = g * 1000;
-  if (tid >= n) {
-    partial[g] = 0.0;
-    pcount[g] = 0;
-    return;
-  }
+__host__ __device__ __forceinline__ uint64_t terms_of_sample(uint64_t g, uint64_t n) {
   const uint64_t t = g % EPS_BLOCK;
-  double s = 0.0;
-  unsigned long long c = 0;
-  for (uint64_t i = t; i < n; i += 1000) {
-    double rd = 0.0;
-    for (uint32_t l = 0; l < d; l++) rd = eps_term(rd, soa[(uint64_t)l * n + i], soa[(uint64_t)l * n + tid]);
-    s = __dadd_rn(s, __dsqrt_rn(rd));
-    c++;
-  }
-  partial[g] = s;
-  pcount[g] = c;
+  return t < n ? (n - t + 999) / 1000 : 0;
 }
 
-__global__ void eps_avg_final_kernel(const double* __restrict__ partial,
-                                     const unsigned long long* __restrict__ pcount, uint64_t nthr,
+template <typename T>
+__global__ void eps_avg_chunk_kernel(const T* __restrict__ soa, uint64_t n, uint32_t d, uint64_t nthr,
+                                     uint32_t nchunks, double* __restrict__ partial) {
+  const uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nthr * nchunks) return;
+  const uint64_t g = w / nchunks;
+  const uint32_t c = (uint32_t)(w % nchunks);
+  const uint64_t tid = g * 1000;
+  double s = 0.0;
+  if (tid < n) {
+    const uint64_t t = g % EPS_BLOCK;
+    const uint64_t m_end = min(terms_of_sample(g, n), (uint64_t)(c + 1) * EPS_CHUNK);
+    for (uint64_t m = (uint64_t)c * EPS_CHUNK; m < m_end; m++) {
+      const uint64_t i = t + 1000 * m;
+      double rd = 0.0;
+      for (uint32_t l = 0; l < d; l++) rd = eps_term(rd, soa[(uint64_t)l * n + i], soa[(uint64_t)l * n + tid]);
+      s = __dadd_rn(s, __dsqrt_rn(rd));
+    }
+  }
+  partial[w] = s;
+}
+
+__global__ void eps_avg_sample_kernel(const double* __restrict__ partial, uint64_t nthr, uint32_t nchunks,
+                                      double* __restrict__ sample_sum) {
+  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nthr) return;
+  double s = 0.0;
+  for (uint32_t c = 0; c < nchunks; c++) s = __dadd_rn(s, partial[g * nchunks + c]);
+  sample_sum[g] = s;
+}
+
+// One warp: the per-sample sums added in sample order.
+__global__ void eps_avg_final_kernel(const double* __restrict__ sample_sum, uint64_t n, uint64_t nthr,
                                      double* __restrict__ out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int lane = threadIdx.x & 31;
   double tot = 0.0;
   unsigned long long cnt = 0;
-  for (uint64_t g = 0; g < nthr; g++) {
-    tot = __dadd_rn(tot, partial[g]);
-    cnt += pcount[g];
+  for (uint64_t b = 0; b < nthr; b += 32) {
+    const uint64_t g = b + lane;
+    const double v = g < nthr ? sample_sum[g] : 0.0;
+#pragma unroll 8
+    for (int j = 0; j < 32; j++) {
+      const double x = __shfl_sync(FULL, v, j);
+      if (b + j < nthr) tot = __dadd_rn(tot, x);
+    }
   }
-  out[0] = __ddiv_rn(tot, (double)cnt);  // GPU.cu:3339: total/(cnt*1.0)
-  out[1] = (double)cnt;
+  for (uint64_t g = 0; g < nthr; g++)
+    if (g * 1000 < n) cnt += terms_of_sample(g, n);
+  if (lane == 0) {
+    out[0] = __ddiv_rn(tot, (double)cnt);  // GPU.cu:3339: total/(cnt*1.0)
+    out[1] = (double)cnt;
+  }
 }
 
 // Exact reference bucket of a squared distance rd (double).  Returns
@@ -89,52 +115,52 @@ __device__ __forceinline__ uint32_t exact_bucket(double rd, double avg, double b
   return b < NBUCKETS ? b : NBUCKETS;
 }
 
+// Counts the buckets in [b_lo, b_hi) of sample blocks.  abs_err bounds the
+// float bracket's absolute distance error from rounding the coordinates to
+// float (0 for float data).
 template <typename T>
-__global__ void __launch_bounds__(EPS_BLOCK) eps_hist_kernel(const T* __restrict__ soa, uint64_t n,
-                                                             uint32_t d, uint32_t offset,
-                                                             const double* __restrict__ avg_in,
-                                                             uint32_t* __restrict__ hist) {
+__global__ void __launch_bounds__(EPS_BLOCK) eps_hist_kernel(const T* __restrict__ soa, uint64_t n, uint32_t d,
+                                                             uint32_t offset, const double* __restrict__ avg_in,
+                                                             uint32_t* __restrict__ hist, uint32_t b_lo,
+                                                             uint32_t b_hi, double abs_err) {
   __shared__ uint32_t sh[NBUCKETS];
-  for (uint32_t i = threadIdx.x; i < NBUCKETS; i += blockDim.x) sh[i] = 0;
+  const uint32_t nb = b_hi - b_lo;
+  for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
   __syncthreads();
   const double avg = avg_in[0];
   const double bw = __ddiv_rn(avg, NBUCKETS * 1.0);  // GPU.cu:3356
   const uint64_t sid = (uint64_t)blockIdx.x * offset;
-  // float bracket (used for float data only)
   const float inv_bw = (float)(1.0 / bw);
-  const float errc = (float)(2 * d + 8) * 5.9604645e-8f;  // (2d+8) * 2^-24
-  const float q_far = 10000.5f;
+  const float errc = (float)(2 * d + 8) * 5.9604645e-8f;  // (2d+8) * 2^-24, relative
+  const float abs_q = (float)(abs_err / bw) * 1.0001f + 1e-4f;
+  const float flo = (float)b_lo, fhi = (float)b_hi;
   for (uint64_t i = 0; i < n; i += (uint64_t)EPS_BLOCK * 8) {
     const uint64_t p = i + threadIdx.x;
     if (p >= n || p == sid) continue;
-    uint32_t bucket = NBUCKETS;
-    if constexpr (sizeof(T) == 4) {
-      float s32 = 0.0f;
-      for (uint32_t l = 0; l < d; l++) {
-        const float df = __fsub_rn((float)soa[(uint64_t)l * n + p], (float)soa[(uint64_t)l * n + sid]);
-        s32 = __fadd_rn(s32, __fmul_rn(df, df));
-      }
-      const float q32 = __fmul_rn(__fsqrt_rn(s32), inv_bw);
-      const float del = __fmaf_rn(errc, q32, 1e-4f);
-      if (q32 - del > q_far) continue;  // certainly not below the mean
-      const float fb = floorf(q32);
-      if (q32 + del < 9999.9f && q32 - del > fb && q32 + del < fb + 1.0f) {
-        bucket = (uint32_t)fb;
-      } else {
-        double rd = 0.0;
-        for (uint32_t l = 0; l < d; l++) rd = eps_term(rd, soa[(uint64_t)l * n + p], soa[(uint64_t)l * n + sid]);
-        bucket = exact_bucket(rd, avg, bw);
-      }
+    float s32 = 0.0f;
+    for (uint32_t l = 0; l < d; l++) {
+      const float df = __fsub_rn((float)soa[(uint64_t)l * n + p], (float)soa[(uint64_t)l * n + sid]);
+      s32 = __fadd_rn(s32, __fmul_rn(df, df));
+    }
+    const float q32 = __fmul_rn(__fsqrt_rn(s32), inv_bw);
+    const float del = __fmaf_rn(errc, q32, abs_q);
+    if (q32 - del >= 10000.5f) continue;  // certainly not below the mean
+    if (q32 + del < flo) continue;        // below this bucket range
+    if (q32 - del >= fhi) continue;       // above this bucket range
+    uint32_t bucket;
+    const float fb = floorf(q32);
+    if (q32 + del < 9999.9f && q32 - del > fb && q32 + del < fb + 1.0f) {
+      bucket = (uint32_t)fb;
     } else {
       double rd = 0.0;
       for (uint32_t l = 0; l < d; l++) rd = eps_term(rd, soa[(uint64_t)l * n + p], soa[(uint64_t)l * n + sid]);
       bucket = exact_bucket(rd, avg, bw);
     }
-    if (bucket < NBUCKETS) atomicAdd(&sh[bucket], 8u);
+    if (bucket >= b_lo && bucket < b_hi) atomicAdd(&sh[bucket - b_lo], 8u);
   }
   __syncthreads();
-  for (uint32_t i = threadIdx.x; i < NBUCKETS; i += blockDim.x)
-    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+  for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[b_lo + i], sh[i]);
 }
 
 }  // namespace
@@ -143,6 +169,11 @@ uint64_t eps_avg_threads(uint64_t n) {
   // GPU.cu:3275: TOTALBLOCKS = ceil((0.001*N)/(1.0*BLOCKSIZE))
   const int blocks = (int)std::ceil((0.001 * (double)(uint32_t)n) / (1.0 * EPS_BLOCK));
   return (uint64_t)blocks * EPS_BLOCK;
+}
+
+uint32_t eps_avg_chunks(uint64_t n) {
+  const uint64_t m = terms_of_sample(0, n);
+  return (uint32_t)std::max<uint64_t>(1, (m + EPS_CHUNK - 1) / EPS_CHUNK);
 }
 
 uint32_t eps_sample_offset(uint64_t n) {
@@ -157,25 +188,36 @@ uint32_t eps_sample_offset(uint64_t n) {
 }
 
 template <typename T>
-void launch_eps(const T* soa, uint64_t n, uint32_t d, const EpsScratch& sc, cudaStream_t s) {
+void launch_eps_avg(const T* soa, uint64_t n, uint32_t d, const EpsScratch& sc, cudaStream_t s) {
   const uint64_t nthr = eps_avg_threads(n);
-  if (nthr > 0) {
-    eps_avg_kernel<T><<<(unsigned)(nthr / EPS_BLOCK), EPS_BLOCK, 0, s>>>(soa, n, d, nthr, sc.partial,
-                                                                      sc.pcount);
+  const uint32_t nch = eps_avg_chunks(n);
+  const uint64_t work = nthr * nch;
+  if (work > 0) {
+    eps_avg_chunk_kernel<T><<<(unsigned)((work + 255) / 256), 256, 0, s>>>(soa, n, d, nthr, nch, sc.partial);
+    KNNSJ_CHECK_LAUNCH();
+    eps_avg_sample_kernel<<<(unsigned)((nthr + 255) / 256), 256, 0, s>>>(sc.partial, nthr, nch, sc.sample_sum);
     KNNSJ_CHECK_LAUNCH();
   }
-  eps_avg_final_kernel<<<1, 32, 0, s>>>(sc.partial, sc.pcount, nthr, sc.avg_out);
+  eps_avg_final_kernel<<<1, 32, 0, s>>>(sc.sample_sum, n, nthr, sc.avg_out);
   KNNSJ_CHECK_LAUNCH();
-  KNNSJ_CUDA(cudaMemsetAsync(sc.hist, 0, NBUCKETS * sizeof(uint32_t), s));
+}
+
+template <typename T>
+void launch_eps_hist(const T* soa, uint64_t n, uint32_t d, const EpsScratch& sc, uint32_t b_lo, uint32_t b_hi,
+                     double abs_err, cudaStream_t s) {
   const uint32_t offset = eps_sample_offset(n);
   const uint32_t blocks2 = (uint32_t)n / offset;  // GPU.cu:3440 (integer division)
-  if (blocks2 > 0) {
-    eps_hist_kernel<T><<<blocks2, EPS_BLOCK, 0, s>>>(soa, n, d, offset, sc.avg_out, sc.hist);
+  if (blocks2 > 0 && b_hi > b_lo) {
+    eps_hist_kernel<T><<<blocks2, EPS_BLOCK, 0, s>>>(soa, n, d, offset, sc.avg_out, sc.hist, b_lo, b_hi, abs_err);
     KNNSJ_CHECK_LAUNCH();
   }
 }
 
-template void launch_eps<float>(const float*, uint64_t, uint32_t, const EpsScratch&, cudaStream_t);
-template void launch_eps<double>(const double*, uint64_t, uint32_t, const EpsScratch&, cudaStream_t);
+template void launch_eps_avg<float>(const float*, uint64_t, uint32_t, const EpsScratch&, cudaStream_t);
+template void launch_eps_avg<double>(const double*, uint64_t, uint32_t, const EpsScratch&, cudaStream_t);
+template void launch_eps_hist<float>(const float*, uint64_t, uint32_t, const EpsScratch&, uint32_t, uint32_t,
+                                     double, cudaStream_t);
+template void launch_eps_hist<double>(const double*, uint64_t, uint32_t, const EpsScratch&, uint32_t, uint32_t,
+                                      double, cudaStream_t);
 
 }  // namespace knnsj

@@ -85,7 +85,48 @@ __global__ void minmax_final_kernel(const T* __restrict__ part, uint32_t nblocks
   out[2 * j + 1] = mx;
 }
 
+constexpr unsigned CHECKSUM_BLOCKS = 1024;
+
+// Squared distance in DTYPE, widened and added in double (GPU.cu:3690-3693);
+// fixed grid, fixed per-thread order and a fixed tree, so the figure is the
+// same on every run.
+template <typename T>
+__global__ void checksum_kernel(const T* __restrict__ v, uint64_t count, double* __restrict__ part) {
+  __shared__ double ws[32];
+  double s = 0.0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const T x = v[i];
+    s = __dadd_rn(s, (double)Num<T>::mul(x, x));
+  }
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(FULL, s, off);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += ws[k];
+    part[blockIdx.x] = t;
+  }
+}
+
+__global__ void checksum_final_kernel(const double* __restrict__ part, unsigned nb, double* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  double t = 0.0;
+  for (unsigned b = 0; b < nb; b++) t += part[b];
+  *out = t;
+}
+
 }  // namespace
+
+template <typename T>
+void launch_checksum(const T* dists, uint64_t count, double* d_partial, double* d_out, cudaStream_t s) {
+  checksum_kernel<T><<<CHECKSUM_BLOCKS, 256, 0, s>>>(dists, count, d_partial);
+  KNNSJ_CHECK_LAUNCH();
+  checksum_final_kernel<<<1, 32, 0, s>>>(d_partial, CHECKSUM_BLOCKS, d_out);
+  KNNSJ_CHECK_LAUNCH();
+}
+template void launch_checksum<float>(const float*, uint64_t, double*, double*, cudaStream_t);
+template void launch_checksum<double>(const double*, uint64_t, double*, double*, cudaStream_t);
 
 constexpr uint32_t MINMAX_BLOCKS = 1024;
 

@@ -7,22 +7,33 @@
 // copy of all pairs (GPU.cu:1671-1676) and the host K-row extraction
 // storeNeighborTableForkNNOnTheFly (GPU.cu:3610-3704).
 //
-// One warp owns one query at a time (dynamic work fetching in chunks).  The
-// warp walks the rows of the query's cell ring -- each row is a run of
-// consecutive linear cell ids, hence one contiguous run of the cell-ordered
-// point array -- with one lane per row doing the cell lookup (dense table or
-// binary search over the non-empty cells, as gridCellLookup does), then
-// streams the concatenated runs 32 points at a time.  Each lane computes one
-// squared distance with the reference's fma chain; points under the current
-// threshold are appended to the warp's shared-memory buffer with one ballot.
-// When the buffer fills, a bitonic sort keeps the K best and tightens the
-// threshold.  A query is accepted when at least K = k+1 points lie within its
-// radius (the reference's acceptance, GPU.cu:3659-3669); otherwise its
-// original id is appended to the failure list for the next, larger radius.
+// One warp owns one query at a time (dynamic work fetching in chunks):
+//   1. In dense-table mode the warp first counts the points of every cell in
+//      the ring (two table reads per row); fewer than K = k+1 means the
+//      query cannot be accepted at this radius and it fails without a scan.
+//   2. The query's own cell is scanned first.
+//   3. The other rows of the ring (a row = consecutive linear cell ids along
+//      dimension 0, one contiguous run of the cell-ordered point array) are
+//      sorted by a lower bound of their distance to the query and scanned in
+//      waves of a few rows.  Once K points are held, a row whose lower bound
+//      exceeds the current K-th distance is skipped, and every row is cut to
+//      the dimension-0 interval that can still hold a better point.
+//   Each lane computes one squared distance with the reference's fma chain
+//   (kernel.cu:139-140); points under the current threshold go to the warp's
+//   shared-memory buffer with one ballot.  When the buffer fills, a 32-bin
+//   histogram of the buffered distances finds a new threshold that keeps at
+//   least K keys (an exact sort when the histogram cannot split them).
+// A query is accepted when at least K points lie within its radius (the
+// reference's acceptance, GPU.cu:3659-3669); its row is then sorted by
+// (distance, id) and written.  Otherwise its original id goes to the failure
+// list for the next, larger radius.
 //
 // Exactness: the ring covers every cell that can hold a point within the
-// radius, including rounding (see cell_range below), so an accepted query's
-// K rows are its exact K nearest by (distance, id).
+// radius, including rounding (cell ranges are widened and rounded outward and
+// mapped through the grid's own monotone cell formula), and every skipped row
+// or cut provably holds no point that could enter the K best, with slack for
+// the rounding of the computed distance.  An accepted query's K rows are its
+// exact K nearest by (computed distance, id) -- the oracle's definition.
 
 #include "knnsj_internal.h"
 
@@ -32,6 +43,10 @@ namespace {
 
 constexpr int SEARCH_THREADS = 256;
 constexpr int QCHUNK = 4;
+constexpr int WAVE_ROWS = 4;          // rows per wave (each gives at most 2 runs)
+constexpr int MAX_RUNS = 2 * WAVE_ROWS;
+constexpr uint32_t HIST_MAX_B = 256;  // histogram reduce for buffers up to this size
+constexpr int WARP_WORDS = 64;        // per-warp u32 scratch: hist[32], runS[8], runP[9]
 
 template <typename T>
 struct SearchParams {
@@ -61,6 +76,21 @@ struct SearchParams {
   uint32_t* work_counter;
 };
 
+// Slack of the pruning bounds: the computed squared distance is within
+// (d+2)*2^-24 (float) or (d+2)*2^-53 (double) of the exact one, d <= 256.
+template <typename T>
+struct Slack;
+template <>
+struct Slack<float> {
+  static constexpr double rel = 1.0 / 16384.0;          // 2^-14
+  static constexpr double cell = 1.0 / 1048576.0;       // 2^-20, cell-boundary fuzz
+};
+template <>
+struct Slack<double> {
+  static constexpr double rel = 1.0 / 1099511627776.0;  // 2^-40
+  static constexpr double cell = 1.0 / 281474976710656.0;  // 2^-48
+};
+
 __device__ __forceinline__ unsigned long long lower_bound_u64(const unsigned long long* __restrict__ a,
                                                               unsigned long long n,
                                                               unsigned long long key) {
@@ -75,22 +105,178 @@ __device__ __forceinline__ unsigned long long lower_bound_u64(const unsigned lon
   return lo;
 }
 
-template <typename T, int D>
-__global__ void __launch_bounds__(SEARCH_THREADS) search_kernel(const SearchParams<T> p) {
+// Points of cells [Llo, Lhi] (consecutive linear ids): one contiguous run.
+template <typename T>
+__device__ __forceinline__ void run_of(const SearchParams<T>& p, unsigned long long Llo, unsigned long long Lhi,
+                                       uint32_t& s, uint32_t& e) {
+  if (Llo > Lhi) {
+    s = e = 0;
+    return;
+  }
+  if (p.dense) {
+    s = p.dstart[Llo];
+    e = p.dstart[Lhi + 1];
+  } else {
+    s = p.coff[lower_bound_u64(p.ckeys, p.C, Llo)];
+    e = p.coff[lower_bound_u64(p.ckeys, p.C, Lhi + 1)];
+  }
+}
+
+__device__ __forceinline__ unsigned long long shfl_key(unsigned long long v, int src) {
+  return __shfl_sync(FULL, v, src);
+}
+__device__ __forceinline__ KeyF64 shfl_key(KeyF64 v, int src) {
+  KeyF64 r;
+  r.a = __shfl_sync(FULL, v.a, src);
+  r.id = __shfl_sync(FULL, v.id, src);
+  r.pad = 0;
+  return r;
+}
+__device__ __forceinline__ unsigned long long key_min() { return 0ull; }
+__device__ __forceinline__ KeyF64 key_min_f64() {
+  KeyF64 k;
+  k.a = 0;
+  k.id = 0;
+  k.pad = 0;
+  return k;
+}
+
+template <typename T>
+struct Sel {
   using K = Key<T>;
   using KT = typename K::type;
+  uint32_t len;
+  KT tau;     // pass iff key < tau
+  bool tight; // tau came from a reduce (an upper bound of the K-th best)
+};
+
+template <typename T>
+__device__ __forceinline__ void sort_reduce(typename Key<T>::type* buf, Sel<T>& st, uint32_t K, uint32_t B,
+                                            int lane) {
+  __syncwarp();
+  for (uint32_t i = st.len + lane; i < B; i += 32) buf[i] = Key<T>::maxv();
+  __syncwarp();
+  warp_bitonic_sort<T>(buf, (int)B, lane);
+  st.len = K;
+  st.tau = buf[K - 1];
+  st.tight = true;
+  __syncwarp();
+}
+
+// Keeps the keys of the lowest histogram bins that hold at least K keys
+// (bins split [0, acc(tau)] evenly); the new threshold is the largest kept
+// key.  Needs st.len >= K and B <= HIST_MAX_B.
+template <typename T>
+__device__ void hist_reduce(typename Key<T>::type* buf, uint32_t* hist, Sel<T>& st, uint32_t K, uint32_t B,
+                            int lane) {
+  using Kt = Key<T>;
+  using KT = typename Kt::type;
+  const double tacc = (double)Kt::acc(st.tau);
+  const double scale = tacc > 0.0 ? 32.0 / tacc : 0.0;
+  __syncwarp();
+  hist[lane] = 0;
+  __syncwarp();
+  for (uint32_t i = lane; i < st.len; i += 32) {
+    const int b = min((int)((double)Kt::acc(buf[i]) * scale), 31);
+    atomicAdd(&hist[b], 1u);
+  }
+  __syncwarp();
+  uint32_t cum = hist[lane];
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t t = __shfl_up_sync(FULL, cum, off);
+    if (lane >= off) cum += t;
+  }
+  const int bst = __ffs(__ballot_sync(FULL, cum >= K)) - 1;
+  const uint32_t kept = __shfl_sync(FULL, cum, bst);
+  if (kept + 32 > B) {  // one bin holds too much: exact reduce
+    sort_reduce<T>(buf, st, K, B, lane);
+    return;
+  }
+  // in-place compaction: a round writes only below the end of what has been
+  // read, so reading the round before writing it is enough
+  uint32_t nl = 0;
+  KT mx;
+  if constexpr (sizeof(KT) == 8)
+    mx = key_min();
+  else
+    mx = key_min_f64();
+  for (uint32_t base = 0; base < st.len; base += 32) {
+    const uint32_t i = base + lane;
+    KT v = Kt::maxv();
+    if (i < st.len) v = buf[i];
+    const bool keep = i < st.len && min((int)((double)Kt::acc(v) * scale), 31) <= bst;
+    const unsigned m = __ballot_sync(FULL, keep);
+    __syncwarp();
+    if (keep) {
+      buf[nl + __popc(m & lanemask_lt())] = v;
+      if (Kt::less(mx, v)) mx = v;
+    }
+    nl += __popc(m);
+    __syncwarp();
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const KT o = shfl_key(mx, lane ^ off);
+    if (Kt::less(mx, o)) mx = o;
+  }
+  st.len = nl;
+  st.tau = mx;
+  st.tight = true;
+  __syncwarp();
+}
+
+template <typename T>
+__device__ __forceinline__ void reduce(typename Key<T>::type* buf, uint32_t* hist, Sel<T>& st, uint32_t K,
+                                       uint32_t B, int lane) {
+  if (B <= HIST_MAX_B)
+    hist_reduce<T>(buf, hist, st, K, B, lane);
+  else
+    sort_reduce<T>(buf, st, K, B, lane);
+}
+
+// Bitonic sort of one 64-bit value per lane across the warp (ascending).
+__device__ __forceinline__ unsigned long long warp_sort32(unsigned long long v, int lane) {
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const unsigned long long o = __shfl_xor_sync(FULL, v, j);
+      const bool up = (lane & k) == 0;
+      const bool low = (lane & j) == 0;
+      const unsigned long long mn = v < o ? v : o;
+      const unsigned long long mx = v < o ? o : v;
+      v = (low == up) ? mn : mx;
+    }
+  }
+  return v;
+}
+
+#ifndef KNNSJ_SEARCH_MIN_BLOCKS
+#define KNNSJ_SEARCH_MIN_BLOCKS 3
+#endif
+
+template <typename T, int D>
+__global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) search_kernel(const SearchParams<T> p) {
+  using Kt = Key<T>;
+  using KT = typename Kt::type;
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   KT* buf = reinterpret_cast<KT*>(smem) + (size_t)wib * p.B;
-  uint32_t* rowS = reinterpret_cast<uint32_t*>(reinterpret_cast<KT*>(smem) + (size_t)wpb * p.B) + wib * 64;
-  uint32_t* rowP = rowS + 32;
+  uint32_t* words = reinterpret_cast<uint32_t*>(reinterpret_cast<KT*>(smem) + (size_t)wpb * p.B) + wib * WARP_WORDS;
+  uint32_t* hist = words;          // [32]
+  uint32_t* runS = words + 32;     // [MAX_RUNS]
+  uint32_t* runP = words + 32 + MAX_RUNS;  // [MAX_RUNS + 1]
   T* qsm = reinterpret_cast<T*>(reinterpret_cast<uint32_t*>(reinterpret_cast<KT*>(smem) + (size_t)wpb * p.B) +
-                                wpb * 64) +
+                                wpb * WARP_WORDS) +
            (size_t)wib * MAX_D;
   const uint64_t n = p.n;
   const uint32_t di = p.g.di;
+  const uint32_t K = p.K;
+  const uint32_t B = p.B;
+  const double wd = (double)p.g.width;
   unsigned long long scanned = 0;
 
   for (;;) {
@@ -113,80 +299,60 @@ __global__ void __launch_bounds__(SEARCH_THREADS) search_kernel(const SearchPara
         for (uint32_t l = lane; l < p.d; l += 32) qsm[l] = qsrc[(uint64_t)l * n + qcol];
         __syncwarp();
       }
+      auto qdim = [&](int j) -> T { return (D > 0) ? q[j < D ? j : 0] : qsm[j]; };
       const T r = p.qradius ? p.qradius[qid] : p.radius;
       const T thr = within_threshold(r);
 
-      // cell_range: any point whose computed squared distance is <= thr
-      // differs from the query by at most r * (1 + 2^-16) (float) in every
-      // coordinate; widen by that, round outward, and map both ends through
-      // the (monotone) cell formula of the grid build.
-      uint32_t lo[MAX_DI], hi[MAX_DI];
+      // cell ring: any point whose computed squared distance is <= thr
+      // differs from the query by at most r * ring_margin per coordinate
+      uint32_t lo[MAX_DI], hi[MAX_DI], own[MAX_DI];
       const double rr = __dmul_ru((double)r, Num<T>::ring_margin);
 #pragma unroll
       for (int j = 0; j < MAX_DI; j++) {
+        lo[j] = hi[j] = own[j] = 0;
         if (j < (int)di) {
-          const T qj = (D > 0) ? q[j < D ? j : 0] : qsm[j];
-          const T lov = Num<T>::down(__dsub_rd((double)qj, rr));
-          const T hiv = Num<T>::up(__dadd_ru((double)qj, rr));
-          lo[j] = clamped_cell(lov, p.g.minv[j], p.g.width, p.g.ncell[j]);
-          hi[j] = clamped_cell(hiv, p.g.minv[j], p.g.width, p.g.ncell[j]);
-        } else {
-          lo[j] = 0;
-          hi[j] = 0;
+          const T qj = qdim(j);
+          lo[j] = clamped_cell(Num<T>::down(__dsub_rd((double)qj, rr)), p.g.minv[j], p.g.width, p.g.ncell[j]);
+          hi[j] = clamped_cell(Num<T>::up(__dadd_ru((double)qj, rr)), p.g.minv[j], p.g.width, p.g.ncell[j]);
+          const uint32_t c = clamped_cell(qj, p.g.minv[j], p.g.width, p.g.ncell[j]);
+          own[j] = c < lo[j] ? lo[j] : (c > hi[j] ? hi[j] : c);
         }
       }
       unsigned long long nrows = 1;
 #pragma unroll
       for (int j = 1; j < MAX_DI; j++)
         if (j < (int)di) nrows *= (unsigned long long)(hi[j] - lo[j] + 1);
+      // row index -> linear id of its dimension-0 origin (cell 0 of the row)
+      auto row_base = [&](unsigned long long ridx, uint32_t* cj) -> unsigned long long {
+        unsigned long long rem = ridx, lin = 0;
+#pragma unroll
+        for (int j = 1; j < MAX_DI; j++) {
+          if (j < (int)di) {
+            const unsigned long long ext = hi[j] - lo[j] + 1;
+            const uint32_t c = lo[j] + (uint32_t)(rem % ext);
+            rem /= ext;
+            cj[j] = c;
+            lin += (unsigned long long)c * p.g.mult[j];
+          }
+        }
+        return lin;
+      };
 
-      KT tau = K::bound(thr);
-      uint32_t len = 0;
-      for (unsigned long long g0 = 0; g0 < nrows; g0 += 32) {
-        const unsigned long long ridx = g0 + lane;
-        uint32_t s = 0, e = 0;
-        if (ridx < nrows) {
-          unsigned long long rem = ridx, lin = 0;
-#pragma unroll
-          for (int j = 1; j < MAX_DI; j++) {
-            if (j < (int)di) {
-              const unsigned long long ext = hi[j] - lo[j] + 1;
-              const unsigned long long c = lo[j] + rem % ext;
-              rem /= ext;
-              lin += c * p.g.mult[j];
-            }
-          }
-          const unsigned long long Llo = lin + lo[0];
-          const unsigned long long Lhi = lin + hi[0];
-          if (p.dense) {
-            s = p.dstart[Llo];
-            e = p.dstart[Lhi + 1];
-          } else {
-            const unsigned long long a = lower_bound_u64(p.ckeys, p.C, Llo);
-            const unsigned long long b = lower_bound_u64(p.ckeys, p.C, Lhi + 1);
-            s = p.coff[a];
-            e = p.coff[b];
-          }
-        }
-        const uint32_t rlen = e - s;
-        uint32_t incl = rlen;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-          const uint32_t t = __shfl_up_sync(FULL, incl, off);
-          if (lane >= off) incl += t;
-        }
-        const uint32_t total = __shfl_sync(FULL, incl, 31);
-        rowS[lane] = s;
-        rowP[lane] = incl - rlen;
-        __syncwarp();
+      Sel<T> st;
+      st.len = 0;
+      st.tau = Kt::bound(thr);
+      st.tight = false;
+
+      // Streams runS/runP[0..nr) (total points) through the selection.
+      auto scan_runs = [&](int nr, uint32_t total) {
         int row = 0;
         for (uint32_t v0 = 0; v0 < total; v0 += 32) {
           const uint32_t v = v0 + lane;
           bool pass = false;
-          KT key = K::maxv();
+          KT key = Kt::maxv();
           if (v < total) {
-            while (row < 31 && rowP[row + 1] <= v) row++;
-            const uint32_t j = rowS[row] + (v - rowP[row]);
+            while (row < nr - 1 && runP[row + 1] <= v) row++;
+            const uint32_t j = runS[row] + (v - runP[row]);
             T acc = 0;
             if (D > 0) {
 #pragma unroll
@@ -200,37 +366,174 @@ __global__ void __launch_bounds__(SEARCH_THREADS) search_kernel(const SearchPara
                 acc = Num<T>::fma(t, t, acc);
               }
             }
-            key = K::make(acc, p.pid[j]);
-            pass = K::less(key, tau);
+            if (acc <= Kt::acc(st.tau)) {
+              key = Kt::make(acc, p.pid[j]);
+              pass = Kt::less(key, st.tau);
+            }
           }
           const unsigned m = __ballot_sync(FULL, pass);
           if (m) {
-            if (pass) buf[len + __popc(m & lanemask_lt())] = key;
-            len += __popc(m);
-            if (len > p.B - 32) {
-              __syncwarp();
-              for (uint32_t i = len + lane; i < p.B; i += 32) buf[i] = K::maxv();
-              __syncwarp();
-              warp_bitonic_sort<T>(buf, (int)p.B, lane);
-              len = p.K;
-              tau = buf[p.K - 1];
-            }
+            if (pass) buf[st.len + __popc(m & lanemask_lt())] = key;
+            st.len += __popc(m);
+            if (st.len > B - 32) reduce<T>(buf, hist, st, K, B, lane);
           }
         }
         scanned += total;
         __syncwarp();
+      };
+      auto tighten = [&]() {
+        if (!st.tight && st.len >= K) reduce<T>(buf, hist, st, K, B, lane);
+      };
+
+      bool fail_now = false;
+      if (p.dense) {
+        uint32_t cnt = 0;
+        for (unsigned long long g0 = 0; g0 < nrows; g0 += 32) {
+          const unsigned long long ridx = g0 + lane;
+          if (ridx < nrows) {
+            uint32_t cj[MAX_DI];
+            const unsigned long long lb = row_base(ridx, cj);
+            cnt += p.dstart[lb + hi[0] + 1] - p.dstart[lb + lo[0]];
+          }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(FULL, cnt, off);
+        fail_now = cnt < K;
       }
+
+      if (!fail_now) {
+        // own cell
+        unsigned long long Lown = 0;
+#pragma unroll
+        for (int j = 0; j < MAX_DI; j++)
+          if (j < (int)di) Lown += (unsigned long long)own[j] * p.g.mult[j];
+        uint32_t s_own, e_own;
+        run_of(p, Lown, Lown, s_own, e_own);
+        if (lane == 0) {
+          runS[0] = s_own;
+          runP[0] = 0;
+          runP[1] = e_own - s_own;
+        }
+        __syncwarp();
+        scan_runs(1, e_own - s_own);
+        tighten();
+
+        // the other rows, nearest first, in waves
+        for (unsigned long long g0 = 0; g0 < nrows; g0 += 32) {
+          const unsigned long long ridx = g0 + lane;
+          double lbq = 1e300;
+          if (ridx < nrows) {
+            uint32_t cj[MAX_DI];
+            row_base(ridx, cj);
+            lbq = 0.0;
+#pragma unroll
+            for (int j = 1; j < MAX_DI; j++) {
+              if (j < (int)di) {
+                const double slo = (double)p.g.minv[j] + (double)cj[j] * wd;
+                const double shi = slo + wd;
+                const double mu = (fabs((double)p.g.minv[j]) + ((double)cj[j] + 1.0) * wd) * Slack<T>::cell;
+                const double qj = (double)qdim(j);
+                const double gap = fmax(0.0, fmax(slo - mu - qj, qj - shi - mu));
+                lbq = __dadd_rd(lbq, __dmul_rd(gap, gap));
+              }
+            }
+          }
+          const float lbf = lbq >= 1e300 ? __int_as_float(0x7f800000) : __double2float_rd(lbq);
+          const unsigned long long skey = warp_sort32(
+              ((unsigned long long)__float_as_uint(lbf) << 32) | (unsigned long long)(uint32_t)lane, lane);
+          const int nvalid = (int)min(32ull, nrows - g0);
+          for (int w0 = 0; w0 < nvalid; w0 += WAVE_ROWS) {
+            const unsigned long long myk = __shfl_sync(FULL, skey, (w0 + lane) & 31);
+            const bool active = lane < WAVE_ROWS && w0 + lane < nvalid;
+            const double tacc = (double)Kt::acc(st.tau);
+            const bool have = st.len >= K;
+            // rows come in ascending lower bound: stop at the first prunable one
+            const float first_lb = __uint_as_float((uint32_t)(__shfl_sync(FULL, myk, 0) >> 32));
+            if (have && (double)first_lb * (1.0 - Slack<T>::rel) > tacc) break;
+            uint32_t sA = 0, eA = 0, sB = 0, eB = 0;
+            if (active) {
+              const unsigned long long rrow = g0 + (uint32_t)(myk & 0xffffffffu);
+              uint32_t cj[MAX_DI];
+              const unsigned long long lb = row_base(rrow, cj);
+              // exact lower bound of this row (dimensions 1..di-1)
+              double lbe = 0.0;
+              bool center = true;
+#pragma unroll
+              for (int j = 1; j < MAX_DI; j++) {
+                if (j < (int)di) {
+                  const double slo = (double)p.g.minv[j] + (double)cj[j] * wd;
+                  const double shi = slo + wd;
+                  const double mu = (fabs((double)p.g.minv[j]) + ((double)cj[j] + 1.0) * wd) * Slack<T>::cell;
+                  const double qj = (double)qdim(j);
+                  const double gap = fmax(0.0, fmax(slo - mu - qj, qj - shi - mu));
+                  lbe = __dadd_rd(lbe, __dmul_rd(gap, gap));
+                  center = center && (cj[j] == own[j]);
+                }
+              }
+              uint32_t xl = lo[0], xh = hi[0];
+              bool empty = false;
+              if (have) {
+                const double lbs = lbe * (1.0 - Slack<T>::rel);
+                if (lbs > tacc) {
+                  empty = true;
+                } else {
+                  const double avail = __dsub_ru(__dmul_ru(tacc, 1.0 + Slack<T>::rel), lbs);
+                  const double g = __dsqrt_ru(fmax(avail, 0.0));
+                  const double q0 = (double)qdim(0);
+                  const uint32_t a0 = clamped_cell(Num<T>::down(__dsub_rd(q0, g)), p.g.minv[0], p.g.width,
+                                                   p.g.ncell[0]);
+                  const uint32_t b0 = clamped_cell(Num<T>::up(__dadd_ru(q0, g)), p.g.minv[0], p.g.width,
+                                                   p.g.ncell[0]);
+                  xl = max(xl, a0);
+                  xh = min(xh, b0);
+                  empty = xl > xh;
+                }
+              }
+              if (!empty) {
+                if (center) {
+                  // the own cell was scanned first
+                  if (own[0] > xl) run_of(p, lb + xl, lb + own[0] - 1, sA, eA);
+                  if (own[0] < xh) run_of(p, lb + own[0] + 1, lb + xh, sB, eB);
+                } else {
+                  run_of(p, lb + xl, lb + xh, sA, eA);
+                }
+              }
+            }
+            const uint32_t la = eA - sA, lbn = eB - sB;
+            uint32_t incl = la + lbn;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+              const uint32_t t = __shfl_up_sync(FULL, incl, off);
+              if (lane >= off) incl += t;
+            }
+            const uint32_t total = __shfl_sync(FULL, incl, WAVE_ROWS - 1);
+            if (lane < WAVE_ROWS) {
+              const uint32_t ex = incl - la - lbn;
+              runS[2 * lane] = sA;
+              runS[2 * lane + 1] = sB;
+              runP[2 * lane] = ex;
+              runP[2 * lane + 1] = ex + la;
+            }
+            __syncwarp();
+            if (total > 0) scan_runs(MAX_RUNS, total);
+            tighten();
+          }
+        }
+      }
+
       __syncwarp();
-      if (len >= p.K) {
+      if (st.len >= K) {
+        if (B <= HIST_MAX_B && st.len > 2 * K && st.len > 64) reduce<T>(buf, hist, st, K, B, lane);
+        const uint32_t len = st.len;
         const uint32_t n2 = len <= 1 ? 1u : (1u << (32 - __clz(len - 1)));
-        for (uint32_t i = len + lane; i < n2; i += 32) buf[i] = K::maxv();
+        for (uint32_t i = len + lane; i < n2; i += 32) buf[i] = Kt::maxv();
         __syncwarp();
         warp_bitonic_sort<T>(buf, (int)n2, lane);
-        const uint64_t row_base = (uint64_t)qid * p.K;
-        for (uint32_t i = lane; i < p.K; i += 32) {
+        const uint64_t row_out = (uint64_t)qid * K;
+        for (uint32_t i = lane; i < K; i += 32) {
           const KT kk = buf[i];
-          p.out_ids[row_base + i] = (int32_t)K::id(kk);
-          p.out_d[row_base + i] = Num<T>::sqrt(K::acc(kk));
+          p.out_ids[row_out + i] = (int32_t)Kt::id(kk);
+          p.out_d[row_out + i] = Num<T>::sqrt(Kt::acc(kk));
         }
       } else if (lane == 0) {
         const uint32_t slot = atomicAdd(p.fail_count, 1u);
@@ -245,9 +548,9 @@ __global__ void __launch_bounds__(SEARCH_THREADS) search_kernel(const SearchPara
 
 template <typename T, int D>
 void launch_one(const SearchParams<T>& prm, int sm_count, cudaStream_t s) {
-  // per-warp shared memory: selection buffer, row table, query copy (generic d)
-  const size_t per_warp =
-      (size_t)prm.B * sizeof(typename Key<T>::type) + 64 * 4 + (D == 0 ? (size_t)MAX_D * sizeof(T) : 0);
+  // per-warp shared memory: selection buffer, u32 scratch, query copy (generic d)
+  const size_t per_warp = (size_t)prm.B * sizeof(typename Key<T>::type) + WARP_WORDS * 4 +
+                          (D == 0 ? (size_t)MAX_D * sizeof(T) : 0);
   int wpb = SEARCH_THREADS / 32;
   while (wpb > 1 && per_warp * wpb > 200 * 1024) wpb--;
   const size_t smem = per_warp * wpb;
@@ -267,8 +570,10 @@ void launch_one(const SearchParams<T>& prm, int sm_count, cudaStream_t s) {
 
 }  // namespace
 
+// Selection buffer per warp: room for K keys plus a full chunk of 32, and at
+// least HIST_MAX_B so the histogram reduce runs rarely.
 int search_buffer_capacity(uint32_t K) {
-  uint32_t b = 64;
+  uint32_t b = HIST_MAX_B;
   while (b < K + 32) b <<= 1;
   return (int)b;
 }

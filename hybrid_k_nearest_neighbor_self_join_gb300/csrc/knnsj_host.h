@@ -73,6 +73,7 @@ struct EpsChoice {
   double eps;
   int bucket;
   uint32_t sample_blocks;
+  bool complete;  // false: the crossing lies beyond the buckets counted so far
 };
 
 inline uint32_t eps_offset_host(uint64_t n) {
@@ -85,17 +86,24 @@ inline uint32_t eps_offset_host(uint64_t n) {
   return (uint32_t)(1.0 / offsetRate);
 }
 
-inline EpsChoice choose_eps(const uint32_t* hist, double avg, uint64_t n, uint32_t k, double beta) {
+// `valid` buckets of hist are counted; when the crossing is not among them
+// (and valid < 10000) the choice is marked incomplete.
+inline EpsChoice choose_eps(const uint32_t* hist, uint32_t valid, double avg, uint64_t n, uint32_t k,
+                            double beta) {
   const uint32_t nbuckets = 10000;
   const double bw = avg / (nbuckets * 1.0);
   const uint32_t blocks2 = (uint32_t)n / eps_offset_host(n);
   uint32_t cumulative = 0;
-  EpsChoice c{0.0, -1, blocks2};
+  EpsChoice c{0.0, -1, blocks2, true};
   bool flag = false;
   const unsigned long min_pts = (unsigned long)(k * 1.0);
   const unsigned long max_pts = (unsigned long)(k * 100.0);
   const unsigned long thr = (unsigned long)(min_pts + (max_pts - min_pts) * beta);
   for (uint32_t i = 0; i < nbuckets; i++) {
+    if (i >= valid) {
+      if (!flag) c.complete = false;
+      break;
+    }
     cumulative += hist[i];
     const double cpp = cumulative / (1.0 * blocks2);
     if (cpp > (double)thr && !flag) {

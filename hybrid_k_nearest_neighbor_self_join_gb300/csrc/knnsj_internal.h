@@ -67,15 +67,23 @@ void launch_minmax(const T* soa, uint64_t n, uint32_t di, T* d_minmax /*2*di*/, 
                    cudaStream_t s);
 
 struct EpsScratch {
-  double* partial = nullptr;            // [n_avg_threads]
-  unsigned long long* pcount = nullptr;  // [n_avg_threads]
-  double* avg_out = nullptr;            // [2]: avg, total count
-  uint32_t* hist = nullptr;             // [10000]
+  double* partial = nullptr;     // [eps_avg_threads * eps_avg_chunks]
+  double* sample_sum = nullptr;  // [eps_avg_threads]
+  double* avg_out = nullptr;     // [2]: mean distance, pair count
+  uint32_t* hist = nullptr;      // [10000]
 };
 uint64_t eps_avg_threads(uint64_t n);
+uint32_t eps_avg_chunks(uint64_t n);
 uint32_t eps_sample_offset(uint64_t n);
 template <typename T>
-void launch_eps(const T* soa, uint64_t n, uint32_t d, const EpsScratch& sc, cudaStream_t s);
+void launch_eps_avg(const T* soa, uint64_t n, uint32_t d, const EpsScratch& sc, cudaStream_t s);
+template <typename T>
+void launch_eps_hist(const T* soa, uint64_t n, uint32_t d, const EpsScratch& sc, uint32_t b_lo, uint32_t b_hi,
+                     double abs_err, cudaStream_t s);
+// Sum of squared result distances (the reference's verification figure,
+// GPU.cu:3690-3693) in a fixed order; result in *d_out.
+template <typename T>
+void launch_checksum(const T* dists, uint64_t count, double* d_partial, double* d_out, cudaStream_t s);
 
 struct GridScratch {
   unsigned long long* keys[2] = {nullptr, nullptr};
@@ -137,7 +145,7 @@ struct Workspace {
   DevBuf xs, ps, pid;                    // input-order columns, cell-order columns, ids
   DevBuf keys0, keys1, vals0, vals1, hist, scan_tmp, flags, pos;  // grid build
   DevBuf ckeys, coff, dstart;            // cell tables
-  DevBuf list0, list1, small, eps_partial, eps_pcount, perm, minmax_part, qradius;
+  DevBuf list0, list1, small, eps_partial, eps_sample, perm, minmax_part, qradius;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   int sm_count = 0;
@@ -156,5 +164,8 @@ struct JoinConfig;
 template <typename T>
 void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
               uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s);
+// Verification figure of a result table on the device (synchronises s).
+template <typename T>
+double device_checksum(Workspace& w, const T* d_vals, uint64_t count, cudaStream_t s);
 
 }  // namespace knnsj

@@ -116,9 +116,10 @@ inline double fma_t(double a, double b, double c) { return std::fma(a, b, c); }
 // kernelKDistBruteForce (kernel.cu:450-523).
 //
 // Deviations, all documented in the returned statistics' meaning:
-//   * the mean distance is summed per sample thread in loop order, then over
-//     sample threads in thread order (the reference uses a double atomicAdd,
-//     whose order -- and so the last bits of the mean -- varies run to run);
+//   * the mean distance is summed per sample thread in chunks of 256 terms
+//     (chunk sums added in order), then over sample threads in thread order
+//     (the reference uses a double atomicAdd, whose order -- and so the last
+//     bits of the mean -- varies run to run);
 //   * histogram reads past N (kernel.cu:486-492 leaves i+threadIdx.x
 //     unchecked) are skipped, and a bucket index that rounds up to nbuckets
 //     is dropped instead of written past the histogram.
@@ -150,15 +151,23 @@ EpsResult estimate_epsilon(const T* X, uint64_t n, uint32_t d, uint32_t k,
     const uint64_t tid = (uint64_t)g * 1000;  // kernel.cu:349
     if (tid >= N) continue;
     const uint32_t t = (uint32_t)(g % BLOCK);  // threadIdx.x
-    double s = 0.0;
+    // fixed summation order: chunks of 256 consecutive terms, chunk sums in
+    // chunk order (the CUDA path sums in exactly this order)
+    const uint64_t chunk = 256;
+    double s = 0.0, cs = 0.0;
     uint64_t c = 0;
     for (uint64_t i = t; i < N; i += 1000) {  // kernel.cu:360
       double rd = 0.0;
       for (uint32_t j = 0; j < d; j++) rd = accum_term(rd, X[i * d + j], X[tid * d + j]);
       rd = std::sqrt(rd);
-      s += rd;
+      cs += rd;
       c++;
+      if (c % chunk == 0) {
+        s += cs;
+        cs = 0.0;
+      }
     }
+    if (c % chunk != 0) s += cs;
     partial[g] = s;
     pcount[g] = c;
   }
