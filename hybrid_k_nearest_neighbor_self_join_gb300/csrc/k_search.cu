@@ -76,21 +76,6 @@ struct SearchParams {
   uint32_t* work_counter;
 };
 
-// Slack of the pruning bounds: the computed squared distance is within
-// (d+2)*2^-24 (float) or (d+2)*2^-53 (double) of the exact one, d <= 256.
-template <typename T>
-struct Slack;
-template <>
-struct Slack<float> {
-  static constexpr double rel = 1.0 / 16384.0;          // 2^-14
-  static constexpr double cell = 1.0 / 1048576.0;       // 2^-20, cell-boundary fuzz
-};
-template <>
-struct Slack<double> {
-  static constexpr double rel = 1.0 / 1099511627776.0;  // 2^-40
-  static constexpr double cell = 1.0 / 281474976710656.0;  // 2^-48
-};
-
 __device__ __forceinline__ unsigned long long lower_bound_u64(const unsigned long long* __restrict__ a,
                                                               unsigned long long n,
                                                               unsigned long long key) {
@@ -141,6 +126,9 @@ __device__ __forceinline__ KeyF64 key_min_f64() {
   return k;
 }
 
+__device__ __forceinline__ float to_float_up(float x) { return x; }
+__device__ __forceinline__ float to_float_up(double x) { return __double2float_ru(x); }
+
 template <typename T>
 struct Sel {
   using K = Key<T>;
@@ -171,13 +159,14 @@ __device__ void hist_reduce(typename Key<T>::type* buf, uint32_t* hist, Sel<T>& 
                             int lane) {
   using Kt = Key<T>;
   using KT = typename Kt::type;
-  const double tacc = (double)Kt::acc(st.tau);
-  const double scale = tacc > 0.0 ? 32.0 / tacc : 0.0;
+  // bins by a monotone float map of the distance: equal distances share a bin
+  const float tacc = to_float_up(Kt::acc(st.tau));
+  const float scale = tacc > 0.0f ? 32.0f / tacc : 0.0f;
   __syncwarp();
   hist[lane] = 0;
   __syncwarp();
   for (uint32_t i = lane; i < st.len; i += 32) {
-    const int b = min((int)((double)Kt::acc(buf[i]) * scale), 31);
+    const int b = min((int)((float)Kt::acc(buf[i]) * scale), 31);
     atomicAdd(&hist[b], 1u);
   }
   __syncwarp();
@@ -205,7 +194,7 @@ __device__ void hist_reduce(typename Key<T>::type* buf, uint32_t* hist, Sel<T>& 
     const uint32_t i = base + lane;
     KT v = Kt::maxv();
     if (i < st.len) v = buf[i];
-    const bool keep = i < st.len && min((int)((double)Kt::acc(v) * scale), 31) <= bst;
+    const bool keep = i < st.len && min((int)((float)Kt::acc(v) * scale), 31) <= bst;
     const unsigned m = __ballot_sync(FULL, keep);
     __syncwarp();
     if (keep) {
@@ -276,7 +265,6 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
   const uint32_t di = p.g.di;
   const uint32_t K = p.K;
   const uint32_t B = p.B;
-  const double wd = (double)p.g.width;
   unsigned long long scanned = 0;
 
   for (;;) {
@@ -303,39 +291,72 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
       const T r = p.qradius ? p.qradius[qid] : p.radius;
       const T thr = within_threshold(r);
 
-      // cell ring: any point whose computed squared distance is <= thr
-      // differs from the query by at most r * ring_margin per coordinate
-      uint32_t lo[MAX_DI], hi[MAX_DI], own[MAX_DI];
-      const double rr = __dmul_ru((double)r, Num<T>::ring_margin);
+      // All bound arithmetic below is float, widened by explicit slack so
+      // that float rounding (and, for double data, the rounding of the
+      // coordinates to float) only ever enlarges what is searched.
+      // Cell ring: a point whose computed squared distance is <= thr differs
+      // from the query by at most r * (1 + 2^-16) per coordinate.
+      const float rf = to_float_up(r) * (1.0f + 1.0f / 8192.0f);
+      uint32_t lo[MAX_DI], hi[MAX_DI], own[MAX_DI], magic[MAX_DI];
+      float qf[MAX_DI];
 #pragma unroll
       for (int j = 0; j < MAX_DI; j++) {
-        lo[j] = hi[j] = own[j] = 0;
+        lo[j] = hi[j] = own[j] = magic[j] = 0;
+        qf[j] = 0.0f;
         if (j < (int)di) {
           const T qj = qdim(j);
-          lo[j] = clamped_cell(Num<T>::down(__dsub_rd((double)qj, rr)), p.g.minv[j], p.g.width, p.g.ncell[j]);
-          hi[j] = clamped_cell(Num<T>::up(__dadd_ru((double)qj, rr)), p.g.minv[j], p.g.width, p.g.ncell[j]);
+          qf[j] = (float)qj;
+          const float slack = (fabsf(qf[j]) + rf) * (1.0f / 2097152.0f);
+          lo[j] = clamped_cell((T)(qf[j] - rf - slack), p.g.minv[j], p.g.width, p.g.ncell[j]);
+          hi[j] = clamped_cell((T)(qf[j] + rf + slack), p.g.minv[j], p.g.width, p.g.ncell[j]);
           const uint32_t c = clamped_cell(qj, p.g.minv[j], p.g.width, p.g.ncell[j]);
           own[j] = c < lo[j] ? lo[j] : (c > hi[j] ? hi[j] : c);
+          const uint32_t ext = hi[j] - lo[j] + 1;
+          magic[j] = ext > 1 ? 0xffffffffu / ext + 1u : 0u;  // x / ext == umulhi(x, magic) for small x
         }
       }
       unsigned long long nrows = 1;
 #pragma unroll
       for (int j = 1; j < MAX_DI; j++)
         if (j < (int)di) nrows *= (unsigned long long)(hi[j] - lo[j] + 1);
-      // row index -> linear id of its dimension-0 origin (cell 0 of the row)
-      auto row_base = [&](unsigned long long ridx, uint32_t* cj) -> unsigned long long {
-        unsigned long long rem = ridx, lin = 0;
+      const float wf = (float)p.g.width;
+
+      // Row ridx of the ring: linear id of its dimension-0 origin, whether it
+      // is the query's own row, and a lower bound of the computed squared
+      // distance of any of its points (dimensions 1..di-1, less 2^-14 for
+      // the rounding of the distance itself).
+      auto row_info = [&](uint32_t ridx, unsigned long long& base, bool& center) -> float {
+        uint32_t rem = ridx;
+        unsigned long long lin = 0;
+        float lbf = 0.0f;
+        center = true;
 #pragma unroll
         for (int j = 1; j < MAX_DI; j++) {
           if (j < (int)di) {
-            const unsigned long long ext = hi[j] - lo[j] + 1;
-            const uint32_t c = lo[j] + (uint32_t)(rem % ext);
-            rem /= ext;
-            cj[j] = c;
+            const uint32_t ext = hi[j] - lo[j] + 1;
+            uint32_t qq = ext > 1 ? __umulhi(rem, magic[j]) : rem;
+            int rj = (int)(rem - qq * ext);
+            if (rj < 0) {
+              qq--;
+              rj += (int)ext;
+            } else if (rj >= (int)ext) {
+              qq++;
+              rj -= (int)ext;
+            }
+            rem = qq;
+            const uint32_t c = lo[j] + (uint32_t)rj;
             lin += (unsigned long long)c * p.g.mult[j];
+            center = center && (c == own[j]);
+            const float mv = (float)p.g.minv[j];
+            const float slo = mv + (float)c * wf;
+            const float shi = slo + wf;
+            const float m = (fabsf(mv) + ((float)c + 1.0f) * wf + fabsf(qf[j])) * (1.0f / 524288.0f);
+            const float gap = fmaxf(0.0f, fmaxf(slo - m - qf[j], qf[j] - shi - m));
+            lbf += gap * gap;
           }
         }
-        return lin;
+        base = lin;
+        return lbf * (1.0f - 1.0f / 16384.0f);
       };
 
       Sel<T> st;
@@ -387,13 +408,15 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
 
       bool fail_now = false;
       if (p.dense) {
+        // fewer than K points in the whole ring: this radius cannot succeed
         uint32_t cnt = 0;
         for (unsigned long long g0 = 0; g0 < nrows; g0 += 32) {
           const unsigned long long ridx = g0 + lane;
           if (ridx < nrows) {
-            uint32_t cj[MAX_DI];
-            const unsigned long long lb = row_base(ridx, cj);
-            cnt += p.dstart[lb + hi[0] + 1] - p.dstart[lb + lo[0]];
+            unsigned long long rb;
+            bool cen;
+            row_info((uint32_t)ridx, rb, cen);
+            cnt += p.dstart[rb + hi[0] + 1] - p.dstart[rb + lo[0]];
           }
         }
 #pragma unroll
@@ -421,69 +444,39 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
         // the other rows, nearest first, in waves
         for (unsigned long long g0 = 0; g0 < nrows; g0 += 32) {
           const unsigned long long ridx = g0 + lane;
-          double lbq = 1e300;
-          if (ridx < nrows) {
-            uint32_t cj[MAX_DI];
-            row_base(ridx, cj);
-            lbq = 0.0;
-#pragma unroll
-            for (int j = 1; j < MAX_DI; j++) {
-              if (j < (int)di) {
-                const double slo = (double)p.g.minv[j] + (double)cj[j] * wd;
-                const double shi = slo + wd;
-                const double mu = (fabs((double)p.g.minv[j]) + ((double)cj[j] + 1.0) * wd) * Slack<T>::cell;
-                const double qj = (double)qdim(j);
-                const double gap = fmax(0.0, fmax(slo - mu - qj, qj - shi - mu));
-                lbq = __dadd_rd(lbq, __dmul_rd(gap, gap));
-              }
-            }
-          }
-          const float lbf = lbq >= 1e300 ? __int_as_float(0x7f800000) : __double2float_rd(lbq);
-          const unsigned long long skey = warp_sort32(
-              ((unsigned long long)__float_as_uint(lbf) << 32) | (unsigned long long)(uint32_t)lane, lane);
+          unsigned long long rbase = 0;
+          bool rcenter = false;
+          float rlb = __int_as_float(0x7f800000);
+          if (ridx < nrows) rlb = row_info((uint32_t)ridx, rbase, rcenter);
+          const unsigned long long skey =
+              warp_sort32(((unsigned long long)__float_as_uint(rlb) << 32) | (unsigned long long)(uint32_t)lane, lane);
           const int nvalid = (int)min(32ull, nrows - g0);
           for (int w0 = 0; w0 < nvalid; w0 += WAVE_ROWS) {
             const unsigned long long myk = __shfl_sync(FULL, skey, (w0 + lane) & 31);
+            const int srcl = (int)(myk & 31u);
+            const unsigned long long lb = __shfl_sync(FULL, rbase, srcl);
+            const bool center = __shfl_sync(FULL, (int)rcenter, srcl) != 0;
+            const float lbs = __uint_as_float((uint32_t)(myk >> 32));
             const bool active = lane < WAVE_ROWS && w0 + lane < nvalid;
-            const double tacc = (double)Kt::acc(st.tau);
+            const float tup = to_float_up(Kt::acc(st.tau));
             const bool have = st.len >= K;
             // rows come in ascending lower bound: stop at the first prunable one
-            const float first_lb = __uint_as_float((uint32_t)(__shfl_sync(FULL, myk, 0) >> 32));
-            if (have && (double)first_lb * (1.0 - Slack<T>::rel) > tacc) break;
+            const float first_lb = __shfl_sync(FULL, lbs, 0);
+            if (have && first_lb > tup) break;
             uint32_t sA = 0, eA = 0, sB = 0, eB = 0;
             if (active) {
-              const unsigned long long rrow = g0 + (uint32_t)(myk & 0xffffffffu);
-              uint32_t cj[MAX_DI];
-              const unsigned long long lb = row_base(rrow, cj);
-              // exact lower bound of this row (dimensions 1..di-1)
-              double lbe = 0.0;
-              bool center = true;
-#pragma unroll
-              for (int j = 1; j < MAX_DI; j++) {
-                if (j < (int)di) {
-                  const double slo = (double)p.g.minv[j] + (double)cj[j] * wd;
-                  const double shi = slo + wd;
-                  const double mu = (fabs((double)p.g.minv[j]) + ((double)cj[j] + 1.0) * wd) * Slack<T>::cell;
-                  const double qj = (double)qdim(j);
-                  const double gap = fmax(0.0, fmax(slo - mu - qj, qj - shi - mu));
-                  lbe = __dadd_rd(lbe, __dmul_rd(gap, gap));
-                  center = center && (cj[j] == own[j]);
-                }
-              }
               uint32_t xl = lo[0], xh = hi[0];
               bool empty = false;
               if (have) {
-                const double lbs = lbe * (1.0 - Slack<T>::rel);
-                if (lbs > tacc) {
+                if (lbs > tup) {
                   empty = true;
                 } else {
-                  const double avail = __dsub_ru(__dmul_ru(tacc, 1.0 + Slack<T>::rel), lbs);
-                  const double g = __dsqrt_ru(fmax(avail, 0.0));
-                  const double q0 = (double)qdim(0);
-                  const uint32_t a0 = clamped_cell(Num<T>::down(__dsub_rd(q0, g)), p.g.minv[0], p.g.width,
-                                                   p.g.ncell[0]);
-                  const uint32_t b0 = clamped_cell(Num<T>::up(__dadd_ru(q0, g)), p.g.minv[0], p.g.width,
-                                                   p.g.ncell[0]);
+                  // dimension-0 interval that can still hold a better point
+                  const float avail = tup * (1.0f + 1.0f / 16384.0f) - lbs;
+                  const float g = sqrtf(fmaxf(avail, 0.0f)) * (1.0f + 1.0f / 1048576.0f);
+                  const float slack = (fabsf(qf[0]) + g) * (1.0f / 2097152.0f);
+                  const uint32_t a0 = clamped_cell((T)(qf[0] - g - slack), p.g.minv[0], p.g.width, p.g.ncell[0]);
+                  const uint32_t b0 = clamped_cell((T)(qf[0] + g + slack), p.g.minv[0], p.g.width, p.g.ncell[0]);
                   xl = max(xl, a0);
                   xh = min(xh, b0);
                   empty = xl > xh;
