@@ -43,10 +43,19 @@ namespace {
 
 constexpr int SEARCH_THREADS = 256;
 constexpr int QCHUNK = 4;
-constexpr int WAVE_ROWS = 4;          // rows per wave (each gives at most 2 runs)
+#ifndef KNNSJ_WAVE_ROWS
+#define KNNSJ_WAVE_ROWS 4
+#endif
+#ifndef KNNSJ_EARLY_FAIL
+#define KNNSJ_EARLY_FAIL 1
+#endif
+#ifndef KNNSJ_SORT_ROWS
+#define KNNSJ_SORT_ROWS 1
+#endif
+constexpr int WAVE_ROWS = KNNSJ_WAVE_ROWS;  // rows per wave (each gives at most 2 runs)
 constexpr int MAX_RUNS = 2 * WAVE_ROWS;
 constexpr uint32_t HIST_MAX_B = 256;  // histogram reduce for buffers up to this size
-constexpr int WARP_WORDS = 64;        // per-warp u32 scratch: hist[32], runS[8], runP[9]
+constexpr int WARP_WORDS = 32 + 2 * MAX_RUNS + 8;  // per-warp u32 scratch: hist, runS, runP
 
 template <typename T>
 struct SearchParams {
@@ -407,7 +416,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
       };
 
       bool fail_now = false;
-      if (p.dense) {
+      if (KNNSJ_EARLY_FAIL && p.dense) {
         // fewer than K points in the whole ring: this radius cannot succeed
         uint32_t cnt = 0;
         for (unsigned long long g0 = 0; g0 < nrows; g0 += 32) {
@@ -448,8 +457,8 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
           bool rcenter = false;
           float rlb = __int_as_float(0x7f800000);
           if (ridx < nrows) rlb = row_info((uint32_t)ridx, rbase, rcenter);
-          const unsigned long long skey =
-              warp_sort32(((unsigned long long)__float_as_uint(rlb) << 32) | (unsigned long long)(uint32_t)lane, lane);
+          unsigned long long skey = ((unsigned long long)__float_as_uint(rlb) << 32) | (unsigned long long)(uint32_t)lane;
+          if (KNNSJ_SORT_ROWS) skey = warp_sort32(skey, lane);
           const int nvalid = (int)min(32ull, nrows - g0);
           for (int w0 = 0; w0 < nvalid; w0 += WAVE_ROWS) {
             const unsigned long long myk = __shfl_sync(FULL, skey, (w0 + lane) & 31);
@@ -462,7 +471,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
             const bool have = st.len >= K;
             // rows come in ascending lower bound: stop at the first prunable one
             const float first_lb = __shfl_sync(FULL, lbs, 0);
-            if (have && first_lb > tup) break;
+            if (KNNSJ_SORT_ROWS && have && first_lb > tup) break;
             uint32_t sA = 0, eA = 0, sB = 0, eB = 0;
             if (active) {
               uint32_t xl = lo[0], xh = hi[0];
