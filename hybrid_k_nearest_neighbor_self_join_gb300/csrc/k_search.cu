@@ -55,7 +55,7 @@ constexpr int QCHUNK = 4;
 constexpr int WAVE_ROWS = KNNSJ_WAVE_ROWS;  // rows per wave (each gives at most 2 runs)
 constexpr int MAX_RUNS = 2 * WAVE_ROWS;
 constexpr uint32_t HIST_MAX_B = 256;  // histogram reduce for buffers up to this size
-constexpr int WARP_WORDS = 32 + 2 * MAX_RUNS + 8;  // per-warp u32 scratch: hist, runS, runP
+constexpr int WARP_WORDS = 256 + 2 * MAX_RUNS + 8;  // per-warp u32 scratch: bins, runS, runP
 
 template <typename T>
 struct SearchParams {
@@ -224,13 +224,119 @@ __device__ void hist_reduce(typename Key<T>::type* buf, uint32_t* hist, Sel<T>& 
   __syncwarp();
 }
 
+// Rare paths are kept out of line so the hot loop stays small in the
+// instruction cache.
 template <typename T>
-__device__ __forceinline__ void reduce(typename Key<T>::type* buf, uint32_t* hist, Sel<T>& st, uint32_t K,
-                                       uint32_t B, int lane) {
+__device__ __noinline__ Sel<T> reduce(typename Key<T>::type* buf, uint32_t* hist, Sel<T> st, uint32_t K, uint32_t B,
+                                      int lane) {
   if (B <= HIST_MAX_B)
     hist_reduce<T>(buf, hist, st, K, B, lane);
   else
     sort_reduce<T>(buf, st, K, B, lane);
+  return st;
+}
+
+// Writes the K smallest of buf[0..len) in ascending (distance, id) order by a
+// counting sort over 256 bins of a monotone map of the distance (all keys are
+// <= acc(top)), ranking keys that share a bin among themselves.  len <= 256.
+template <typename T>
+__device__ __noinline__ void write_sorted_row(typename Key<T>::type* buf, uint32_t* cnt, uint32_t len,
+                                              typename Key<T>::type top, uint32_t K, int32_t* __restrict__ out_ids,
+                                              T* __restrict__ out_d, uint64_t row_out, int lane) {
+  using Kt = Key<T>;
+  using KT = typename Kt::type;
+  constexpr int R = HIST_MAX_B / 32;
+  const float tacc = to_float_up(Kt::acc(top));
+  const float scale = tacc > 0.0f ? 256.0f / tacc : 0.0f;
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 8; r++) cnt[r * 32 + lane] = 0;
+  __syncwarp();
+  KT v[R];
+  uint32_t slot[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const uint32_t i = r * 32 + lane;
+    v[r] = Kt::maxv();
+    slot[r] = 0;
+    if (i < len) {
+      v[r] = buf[i];
+      const int b = min((int)((float)Kt::acc(v[r]) * scale), 255);
+      slot[r] = atomicAdd(&cnt[b], 1u);
+    }
+  }
+  __syncwarp();
+  // exclusive scan of the 256 bin counts, 8 consecutive bins per lane
+  uint32_t c[8], s = 0;
+#pragma unroll
+  for (int t = 0; t < 8; t++) {
+    c[t] = cnt[lane * 8 + t];
+    s += c[t];
+  }
+  uint32_t incl = s;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t t = __shfl_up_sync(FULL, incl, off);
+    if (lane >= off) incl += t;
+  }
+  uint32_t run = incl - s;
+  __syncwarp();
+#pragma unroll
+  for (int t = 0; t < 8; t++) {
+    cnt[lane * 8 + t] = run;
+    run += c[t];
+  }
+  __syncwarp();
+  // scatter by bin (order inside a bin still arbitrary)
+  uint32_t pos[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const uint32_t i = r * 32 + lane;
+    pos[r] = 0xffffffffu;
+    if (i < len) {
+      const int b = min((int)((float)Kt::acc(v[r]) * scale), 255);
+      pos[r] = cnt[b] + slot[r];
+      buf[pos[r]] = v[r];
+    }
+  }
+  __syncwarp();
+  // rank inside the bin, then write rows below K
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const uint32_t i = r * 32 + lane;
+    if (i < len) {
+      const int b = min((int)((float)Kt::acc(v[r]) * scale), 255);
+      const uint32_t first = cnt[b];
+      const uint32_t last = b < 255 ? cnt[b + 1] : len;
+      uint32_t rank = 0;
+      for (uint32_t j = first; j < last; j++) rank += Kt::less(buf[j], v[r]) ? 1u : 0u;
+      const uint32_t fin = first + rank;
+      if (fin < K) {
+        out_ids[row_out + fin] = (int32_t)Kt::id(v[r]);
+        out_d[row_out + fin] = Num<T>::sqrt(Kt::acc(v[r]));
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// Writes the K smallest of buf[0..len) by a full bitonic sort (any len <= B).
+template <typename T>
+__device__ __noinline__ void write_sorted_row_bitonic(typename Key<T>::type* buf, uint32_t len, uint32_t K,
+                                                      int32_t* __restrict__ out_ids, T* __restrict__ out_d,
+                                                      uint64_t row_out, int lane) {
+  using Kt = Key<T>;
+  const uint32_t n2 = len <= 1 ? 1u : (1u << (32 - __clz(len - 1)));
+  __syncwarp();
+  for (uint32_t i = len + lane; i < n2; i += 32) buf[i] = Kt::maxv();
+  __syncwarp();
+  warp_bitonic_sort<T>(buf, (int)n2, lane);
+  for (uint32_t i = lane; i < K; i += 32) {
+    const typename Kt::type kk = buf[i];
+    out_ids[row_out + i] = (int32_t)Kt::id(kk);
+    out_d[row_out + i] = Num<T>::sqrt(Kt::acc(kk));
+  }
+  __syncwarp();
 }
 
 // Bitonic sort of one 64-bit value per lane across the warp (ascending).
@@ -254,8 +360,10 @@ __device__ __forceinline__ unsigned long long warp_sort32(unsigned long long v, 
 #define KNNSJ_SEARCH_MIN_BLOCKS 3
 #endif
 
-template <typename T, int D>
+// D: data dimensions (0 = runtime); DI: indexed dimensions (0 = runtime, <= MAX_DI).
+template <typename T, int D, int DI>
 __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) search_kernel(const SearchParams<T> p) {
+  constexpr int NDI = DI > 0 ? DI : MAX_DI;
   using Kt = Key<T>;
   using KT = typename Kt::type;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -264,14 +372,14 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
   const int wpb = blockDim.x >> 5;
   KT* buf = reinterpret_cast<KT*>(smem) + (size_t)wib * p.B;
   uint32_t* words = reinterpret_cast<uint32_t*>(reinterpret_cast<KT*>(smem) + (size_t)wpb * p.B) + wib * WARP_WORDS;
-  uint32_t* hist = words;          // [32]
-  uint32_t* runS = words + 32;     // [MAX_RUNS]
-  uint32_t* runP = words + 32 + MAX_RUNS;  // [MAX_RUNS + 1]
+  uint32_t* hist = words;                   // [256]: reduce bins / output counting sort
+  uint32_t* runS = words + 256;             // [MAX_RUNS]
+  uint32_t* runP = words + 256 + MAX_RUNS;  // [MAX_RUNS + 1]
   T* qsm = reinterpret_cast<T*>(reinterpret_cast<uint32_t*>(reinterpret_cast<KT*>(smem) + (size_t)wpb * p.B) +
                                 wpb * WARP_WORDS) +
            (size_t)wib * MAX_D;
   const uint64_t n = p.n;
-  const uint32_t di = p.g.di;
+  const uint32_t di = DI > 0 ? (uint32_t)DI : p.g.di;
   const uint32_t K = p.K;
   const uint32_t B = p.B;
   unsigned long long scanned = 0;
@@ -306,10 +414,10 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
       // Cell ring: a point whose computed squared distance is <= thr differs
       // from the query by at most r * (1 + 2^-16) per coordinate.
       const float rf = to_float_up(r) * (1.0f + 1.0f / 8192.0f);
-      uint32_t lo[MAX_DI], hi[MAX_DI], own[MAX_DI], magic[MAX_DI];
-      float qf[MAX_DI];
+      uint32_t lo[NDI], hi[NDI], own[NDI], magic[NDI];
+      float qf[NDI];
 #pragma unroll
-      for (int j = 0; j < MAX_DI; j++) {
+      for (int j = 0; j < NDI; j++) {
         lo[j] = hi[j] = own[j] = magic[j] = 0;
         qf[j] = 0.0f;
         if (j < (int)di) {
@@ -326,7 +434,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
       }
       unsigned long long nrows = 1;
 #pragma unroll
-      for (int j = 1; j < MAX_DI; j++)
+      for (int j = 1; j < NDI; j++)
         if (j < (int)di) nrows *= (unsigned long long)(hi[j] - lo[j] + 1);
       const float wf = (float)p.g.width;
 
@@ -334,13 +442,13 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
       // is the query's own row, and a lower bound of the computed squared
       // distance of any of its points (dimensions 1..di-1, less 2^-14 for
       // the rounding of the distance itself).
-      auto row_info = [&](uint32_t ridx, unsigned long long& base, bool& center) -> float {
+      auto row_info = [&](uint32_t ridx, unsigned long long& rbase, bool& center) -> float {
         uint32_t rem = ridx;
         unsigned long long lin = 0;
         float lbf = 0.0f;
         center = true;
 #pragma unroll
-        for (int j = 1; j < MAX_DI; j++) {
+        for (int j = 1; j < NDI; j++) {
           if (j < (int)di) {
             const uint32_t ext = hi[j] - lo[j] + 1;
             uint32_t qq = ext > 1 ? __umulhi(rem, magic[j]) : rem;
@@ -364,7 +472,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
             lbf += gap * gap;
           }
         }
-        base = lin;
+        rbase = lin;
         return lbf * (1.0f - 1.0f / 16384.0f);
       };
 
@@ -373,8 +481,126 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
       st.tau = Kt::bound(thr);
       st.tight = false;
 
-      // Streams runS/runP[0..nr) (total points) through the selection.
-      auto scan_runs = [&](int nr, uint32_t total) {
+      bool fail_now = false;
+      if (KNNSJ_EARLY_FAIL && p.dense) {
+        // fewer than K points in the whole ring: this radius cannot succeed
+        uint32_t cnt = 0;
+        for (unsigned long long g0 = 0; g0 < nrows; g0 += 32) {
+          const unsigned long long ridx = g0 + lane;
+          if (ridx < nrows) {
+            unsigned long long rb;
+            bool cen;
+            row_info((uint32_t)ridx, rb, cen);
+            cnt += p.dstart[rb + hi[0] + 1] - p.dstart[rb + lo[0]];
+          }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(FULL, cnt, off);
+        fail_now = cnt < K;
+      }
+
+      // Producer of run lists: first the query's own cell, then the other
+      // rows of the ring in groups of 32 sorted by lower bound, a wave of
+      // WAVE_ROWS rows at a time.  One scan loop consumes them all.
+      bool own_pending = !fail_now;
+      unsigned long long g0 = 0;   // first row of the current group
+      int nvalid = 0, w0 = 0;      // rows in the group, next wave start
+      unsigned long long skey = 0, rbase = 0;
+      bool rcenter = false;
+      const unsigned long long groups_end = fail_now ? 0 : nrows;
+      for (;;) {
+        uint32_t total = 0;
+        int nr = 1;
+        if (own_pending) {
+          own_pending = false;
+          unsigned long long Lown = 0;
+#pragma unroll
+          for (int j = 0; j < NDI; j++)
+            if (j < (int)di) Lown += (unsigned long long)own[j] * p.g.mult[j];
+          uint32_t s_own, e_own;
+          run_of(p, Lown, Lown, s_own, e_own);
+          if (lane == 0) {
+            runS[0] = s_own;
+            runP[0] = 0;
+          }
+          total = e_own - s_own;
+        } else {
+          if (w0 >= nvalid) {  // next group of rows
+            if (nvalid > 0) g0 += 32;
+            if (g0 >= groups_end) break;
+            const unsigned long long ridx = g0 + lane;
+            float rlb = __int_as_float(0x7f800000);
+            rbase = 0;
+            rcenter = false;
+            if (ridx < nrows) rlb = row_info((uint32_t)ridx, rbase, rcenter);
+            skey = ((unsigned long long)__float_as_uint(rlb) << 32) | (unsigned long long)(uint32_t)lane;
+            if (KNNSJ_SORT_ROWS) skey = warp_sort32(skey, lane);
+            nvalid = (int)min(32ull, nrows - g0);
+            w0 = 0;
+          }
+          const unsigned long long myk = __shfl_sync(FULL, skey, (w0 + lane) & 31);
+          const int srcl = (int)(myk & 31u);
+          const unsigned long long lb = __shfl_sync(FULL, rbase, srcl);
+          const bool center = __shfl_sync(FULL, (int)rcenter, srcl) != 0;
+          const float lbs = __uint_as_float((uint32_t)(myk >> 32));
+          const bool active = lane < WAVE_ROWS && w0 + lane < nvalid;
+          const float tup = to_float_up(Kt::acc(st.tau));
+          const bool have = st.len >= K;
+          // rows come in ascending lower bound: the rest of the group can go
+          const float first_lb = __shfl_sync(FULL, lbs, 0);
+          if (KNNSJ_SORT_ROWS && have && first_lb > tup) {
+            w0 = nvalid;
+            continue;
+          }
+          uint32_t sA = 0, eA = 0, sB = 0, eB = 0;
+          if (active) {
+            uint32_t xl = lo[0], xh = hi[0];
+            bool empty = false;
+            if (have) {
+              if (lbs > tup) {
+                empty = true;
+              } else {
+                // dimension-0 interval that can still hold a better point
+                const float avail = tup * (1.0f + 1.0f / 16384.0f) - lbs;
+                const float g = sqrtf(fmaxf(avail, 0.0f)) * (1.0f + 1.0f / 1048576.0f);
+                const float slack = (fabsf(qf[0]) + g) * (1.0f / 2097152.0f);
+                const uint32_t a0 = clamped_cell((T)(qf[0] - g - slack), p.g.minv[0], p.g.width, p.g.ncell[0]);
+                const uint32_t b0 = clamped_cell((T)(qf[0] + g + slack), p.g.minv[0], p.g.width, p.g.ncell[0]);
+                xl = max(xl, a0);
+                xh = min(xh, b0);
+                empty = xl > xh;
+              }
+            }
+            if (!empty) {
+              if (center) {
+                // the own cell was scanned first
+                if (own[0] > xl) run_of(p, lb + xl, lb + own[0] - 1, sA, eA);
+                if (own[0] < xh) run_of(p, lb + own[0] + 1, lb + xh, sB, eB);
+              } else {
+                run_of(p, lb + xl, lb + xh, sA, eA);
+              }
+            }
+          }
+          const uint32_t la = eA - sA, lbn = eB - sB;
+          uint32_t incl = la + lbn;
+#pragma unroll
+          for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t t = __shfl_up_sync(FULL, incl, off);
+            if (lane >= off) incl += t;
+          }
+          total = __shfl_sync(FULL, incl, WAVE_ROWS - 1);
+          if (lane < WAVE_ROWS) {
+            const uint32_t ex = incl - la - lbn;
+            runS[2 * lane] = sA;
+            runS[2 * lane + 1] = sB;
+            runP[2 * lane] = ex;
+            runP[2 * lane + 1] = ex + la;
+          }
+          nr = MAX_RUNS;
+          w0 += WAVE_ROWS;
+        }
+        __syncwarp();
+        // the scan: one squared distance per lane, ballot-append under tau
         int row = 0;
         for (uint32_t v0 = 0; v0 < total; v0 += 32) {
           const uint32_t v = v0 + lane;
@@ -405,137 +631,22 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
           if (m) {
             if (pass) buf[st.len + __popc(m & lanemask_lt())] = key;
             st.len += __popc(m);
-            if (st.len > B - 32) reduce<T>(buf, hist, st, K, B, lane);
+            if (st.len > B - 32) st = reduce<T>(buf, hist, st, K, B, lane);
           }
         }
         scanned += total;
         __syncwarp();
-      };
-      auto tighten = [&]() {
-        if (!st.tight && st.len >= K) reduce<T>(buf, hist, st, K, B, lane);
-      };
-
-      bool fail_now = false;
-      if (KNNSJ_EARLY_FAIL && p.dense) {
-        // fewer than K points in the whole ring: this radius cannot succeed
-        uint32_t cnt = 0;
-        for (unsigned long long g0 = 0; g0 < nrows; g0 += 32) {
-          const unsigned long long ridx = g0 + lane;
-          if (ridx < nrows) {
-            unsigned long long rb;
-            bool cen;
-            row_info((uint32_t)ridx, rb, cen);
-            cnt += p.dstart[rb + hi[0] + 1] - p.dstart[rb + lo[0]];
-          }
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(FULL, cnt, off);
-        fail_now = cnt < K;
-      }
-
-      if (!fail_now) {
-        // own cell
-        unsigned long long Lown = 0;
-#pragma unroll
-        for (int j = 0; j < MAX_DI; j++)
-          if (j < (int)di) Lown += (unsigned long long)own[j] * p.g.mult[j];
-        uint32_t s_own, e_own;
-        run_of(p, Lown, Lown, s_own, e_own);
-        if (lane == 0) {
-          runS[0] = s_own;
-          runP[0] = 0;
-          runP[1] = e_own - s_own;
-        }
-        __syncwarp();
-        scan_runs(1, e_own - s_own);
-        tighten();
-
-        // the other rows, nearest first, in waves
-        for (unsigned long long g0 = 0; g0 < nrows; g0 += 32) {
-          const unsigned long long ridx = g0 + lane;
-          unsigned long long rbase = 0;
-          bool rcenter = false;
-          float rlb = __int_as_float(0x7f800000);
-          if (ridx < nrows) rlb = row_info((uint32_t)ridx, rbase, rcenter);
-          unsigned long long skey = ((unsigned long long)__float_as_uint(rlb) << 32) | (unsigned long long)(uint32_t)lane;
-          if (KNNSJ_SORT_ROWS) skey = warp_sort32(skey, lane);
-          const int nvalid = (int)min(32ull, nrows - g0);
-          for (int w0 = 0; w0 < nvalid; w0 += WAVE_ROWS) {
-            const unsigned long long myk = __shfl_sync(FULL, skey, (w0 + lane) & 31);
-            const int srcl = (int)(myk & 31u);
-            const unsigned long long lb = __shfl_sync(FULL, rbase, srcl);
-            const bool center = __shfl_sync(FULL, (int)rcenter, srcl) != 0;
-            const float lbs = __uint_as_float((uint32_t)(myk >> 32));
-            const bool active = lane < WAVE_ROWS && w0 + lane < nvalid;
-            const float tup = to_float_up(Kt::acc(st.tau));
-            const bool have = st.len >= K;
-            // rows come in ascending lower bound: stop at the first prunable one
-            const float first_lb = __shfl_sync(FULL, lbs, 0);
-            if (KNNSJ_SORT_ROWS && have && first_lb > tup) break;
-            uint32_t sA = 0, eA = 0, sB = 0, eB = 0;
-            if (active) {
-              uint32_t xl = lo[0], xh = hi[0];
-              bool empty = false;
-              if (have) {
-                if (lbs > tup) {
-                  empty = true;
-                } else {
-                  // dimension-0 interval that can still hold a better point
-                  const float avail = tup * (1.0f + 1.0f / 16384.0f) - lbs;
-                  const float g = sqrtf(fmaxf(avail, 0.0f)) * (1.0f + 1.0f / 1048576.0f);
-                  const float slack = (fabsf(qf[0]) + g) * (1.0f / 2097152.0f);
-                  const uint32_t a0 = clamped_cell((T)(qf[0] - g - slack), p.g.minv[0], p.g.width, p.g.ncell[0]);
-                  const uint32_t b0 = clamped_cell((T)(qf[0] + g + slack), p.g.minv[0], p.g.width, p.g.ncell[0]);
-                  xl = max(xl, a0);
-                  xh = min(xh, b0);
-                  empty = xl > xh;
-                }
-              }
-              if (!empty) {
-                if (center) {
-                  // the own cell was scanned first
-                  if (own[0] > xl) run_of(p, lb + xl, lb + own[0] - 1, sA, eA);
-                  if (own[0] < xh) run_of(p, lb + own[0] + 1, lb + xh, sB, eB);
-                } else {
-                  run_of(p, lb + xl, lb + xh, sA, eA);
-                }
-              }
-            }
-            const uint32_t la = eA - sA, lbn = eB - sB;
-            uint32_t incl = la + lbn;
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-              const uint32_t t = __shfl_up_sync(FULL, incl, off);
-              if (lane >= off) incl += t;
-            }
-            const uint32_t total = __shfl_sync(FULL, incl, WAVE_ROWS - 1);
-            if (lane < WAVE_ROWS) {
-              const uint32_t ex = incl - la - lbn;
-              runS[2 * lane] = sA;
-              runS[2 * lane + 1] = sB;
-              runP[2 * lane] = ex;
-              runP[2 * lane + 1] = ex + la;
-            }
-            __syncwarp();
-            if (total > 0) scan_runs(MAX_RUNS, total);
-            tighten();
-          }
-        }
+        if (!st.tight && st.len >= K) st = reduce<T>(buf, hist, st, K, B, lane);
       }
 
       __syncwarp();
       if (st.len >= K) {
-        if (B <= HIST_MAX_B && st.len > 2 * K && st.len > 64) reduce<T>(buf, hist, st, K, B, lane);
-        const uint32_t len = st.len;
-        const uint32_t n2 = len <= 1 ? 1u : (1u << (32 - __clz(len - 1)));
-        for (uint32_t i = len + lane; i < n2; i += 32) buf[i] = Kt::maxv();
-        __syncwarp();
-        warp_bitonic_sort<T>(buf, (int)n2, lane);
         const uint64_t row_out = (uint64_t)qid * K;
-        for (uint32_t i = lane; i < K; i += 32) {
-          const KT kk = buf[i];
-          p.out_ids[row_out + i] = (int32_t)Kt::id(kk);
-          p.out_d[row_out + i] = Num<T>::sqrt(Kt::acc(kk));
+        if (B <= HIST_MAX_B) {
+          if (st.len > 2 * K && st.len > 64) st = reduce<T>(buf, hist, st, K, B, lane);
+          write_sorted_row<T>(buf, hist, st.len, st.tau, K, p.out_ids, p.out_d, row_out, lane);
+        } else {
+          write_sorted_row_bitonic<T>(buf, st.len, K, p.out_ids, p.out_d, row_out, lane);
         }
       } else if (lane == 0) {
         const uint32_t slot = atomicAdd(p.fail_count, 1u);
@@ -548,7 +659,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
   if (lane == 0 && scanned) atomicAdd(p.cand_count, scanned);
 }
 
-template <typename T, int D>
+template <typename T, int D, int DI>
 void launch_one(const SearchParams<T>& prm, int sm_count, cudaStream_t s) {
   // per-warp shared memory: selection buffer, u32 scratch, query copy (generic d)
   const size_t per_warp = (size_t)prm.B * sizeof(typename Key<T>::type) + WARP_WORDS * 4 +
@@ -556,7 +667,7 @@ void launch_one(const SearchParams<T>& prm, int sm_count, cudaStream_t s) {
   int wpb = SEARCH_THREADS / 32;
   while (wpb > 1 && per_warp * wpb > 200 * 1024) wpb--;
   const size_t smem = per_warp * wpb;
-  auto kern = search_kernel<T, D>;
+  auto kern = search_kernel<T, D, DI>;
   KNNSJ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   KNNSJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, wpb * 32, smem));
@@ -609,15 +720,16 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s) {
   p.cand_count = a.cand_count;
   p.work_counter = a.work_counter;
   KNNSJ_CUDA(cudaMemsetAsync(a.work_counter, 0, sizeof(uint32_t), s));
+  const bool full = a.grid.geom.di == a.d;  // every dimension indexed
   switch (a.d) {
-    case 2: launch_one<T, 2>(p, sm_count, s); break;
-    case 3: launch_one<T, 3>(p, sm_count, s); break;
-    case 4: launch_one<T, 4>(p, sm_count, s); break;
-    case 5: launch_one<T, 5>(p, sm_count, s); break;
-    case 6: launch_one<T, 6>(p, sm_count, s); break;
-    case 7: launch_one<T, 7>(p, sm_count, s); break;
-    case 8: launch_one<T, 8>(p, sm_count, s); break;
-    default: launch_one<T, 0>(p, sm_count, s); break;
+    case 2: full ? launch_one<T, 2, 2>(p, sm_count, s) : launch_one<T, 2, 0>(p, sm_count, s); break;
+    case 3: full ? launch_one<T, 3, 3>(p, sm_count, s) : launch_one<T, 3, 0>(p, sm_count, s); break;
+    case 4: full ? launch_one<T, 4, 4>(p, sm_count, s) : launch_one<T, 4, 0>(p, sm_count, s); break;
+    case 5: full ? launch_one<T, 5, 5>(p, sm_count, s) : launch_one<T, 5, 0>(p, sm_count, s); break;
+    case 6: full ? launch_one<T, 6, 6>(p, sm_count, s) : launch_one<T, 6, 0>(p, sm_count, s); break;
+    case 7: full ? launch_one<T, 7, 7>(p, sm_count, s) : launch_one<T, 7, 0>(p, sm_count, s); break;
+    case 8: full ? launch_one<T, 8, 8>(p, sm_count, s) : launch_one<T, 8, 0>(p, sm_count, s); break;
+    default: launch_one<T, 0, 0>(p, sm_count, s); break;
   }
 }
 
