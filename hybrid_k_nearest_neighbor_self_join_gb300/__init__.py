@@ -32,14 +32,19 @@ def version() -> str:
     return _lib.load().knnsj_version().decode()
 
 
+RADIUS_PLAIN = _lib.KNNSJ_RADIUS_BETA
+RADIUS_LEARNED = _lib.KNNSJ_RADIUS_LEARNED
+
+
 def selfjoin(data: np.ndarray, k: int, *, num_indexed_dims: int = 0, beta: float | None = None,
              reorder: bool = True, radius_mode: int = 0, max_iterations: int = 0, device: int = -1,
-             out_ids: np.ndarray | None = None, out_dists: np.ndarray | None = None,
-             return_stats: bool = False):
+             radius_offset: float = 0.0, out_ids: np.ndarray | None = None,
+             out_dists: np.ndarray | None = None, return_stats: bool = False):
     """Exact kNN self-join of row-major host data (N x d, float32/float64).
 
     Returns (ids, dists), each (N, k+1): row q holds the k+1 nearest points of
     point q, itself included, by ascending distance (ties by id).
+    radius_mode: RADIUS_PLAIN (the reference's BETA rule) or RADIUS_LEARNED.
     """
     x = np.ascontiguousarray(data)
     if x.ndim != 2:
@@ -48,7 +53,8 @@ def selfjoin(data: np.ndarray, k: int, *, num_indexed_dims: int = 0, beta: float
     K = k + 1
     ids = out_ids if out_ids is not None else np.empty((n, K), np.int32)
     dists = out_dists if out_dists is not None else np.empty((n, K), x.dtype)
-    opts = Options.make(num_indexed_dims, beta, reorder, radius_mode, max_iterations, device)
+    opts = Options.make(num_indexed_dims, beta, reorder, radius_mode, max_iterations, device,
+                        radius_offset=radius_offset)
     st = Stats.make()
     lib = _lib.load()
     rc = lib.knnsj_selfjoin(x.ctypes.data, _dtype_code(x.dtype), n, d, k, ctypes.byref(opts),
@@ -59,9 +65,10 @@ def selfjoin(data: np.ndarray, k: int, *, num_indexed_dims: int = 0, beta: float
 
 def selfjoin_device(data_ptr: int, dtype, n: int, d: int, k: int, ids_ptr: int, dists_ptr: int, *,
                     num_indexed_dims: int = 0, beta: float | None = None, reorder: bool = True,
-                    radius_mode: int = 0, max_iterations: int = 0) -> dict:
+                    radius_mode: int = 0, max_iterations: int = 0, radius_offset: float = 0.0) -> dict:
     """Self-join on device pointers (e.g. torch.Tensor.data_ptr()); returns stats."""
-    opts = Options.make(num_indexed_dims, beta, reorder, radius_mode, max_iterations, -1)
+    opts = Options.make(num_indexed_dims, beta, reorder, radius_mode, max_iterations, -1,
+                        radius_offset=radius_offset)
     st = Stats.make()
     rc = _lib.load().knnsj_selfjoin_device(ctypes.c_void_p(data_ptr), _dtype_code(dtype), n, d, k,
                                            ctypes.byref(opts), ctypes.c_void_p(ids_ptr),
@@ -97,6 +104,24 @@ def selfjoin_batched(datasets, ks, *, beta: float | None = None, radius_mode: in
                                             ctypes.byref(st))
     _lib.check(rc, "knnsj_selfjoin_batched")
     return outs
+
+
+def get_radius_model() -> np.ndarray:
+    """The active learned-radius model (5873 floats)."""
+    m = np.empty(_lib.RADIUS_MODEL_FLOATS, np.float32)
+    _lib.check(_lib.load().knnsj_get_radius_model(m.ctypes.data))
+    return m
+
+
+def set_radius_model(model: np.ndarray | None) -> None:
+    """Replaces the active learned-radius model; None restores the built-in one."""
+    if model is None:
+        _lib.check(_lib.load().knnsj_set_radius_model(None))
+        return
+    m = np.ascontiguousarray(model, np.float32)
+    if m.size != _lib.RADIUS_MODEL_FLOATS:
+        raise ValueError("model must have 5873 floats")
+    _lib.check(_lib.load().knnsj_set_radius_model(m.ctypes.data))
 
 
 def reorder_dims(data: np.ndarray):

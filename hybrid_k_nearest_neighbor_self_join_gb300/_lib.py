@@ -42,12 +42,13 @@ class Options(ctypes.Structure):
         ("max_iterations", ctypes.c_int32),
         ("device", ctypes.c_int32),
         ("verbose", ctypes.c_int32),
+        ("radius_offset", ctypes.c_double),
         ("reserved", ctypes.c_int32 * 8),
     ]
 
     @classmethod
     def make(cls, num_indexed_dims=0, beta=None, reorder=True, radius_mode=0, max_iterations=0,
-             device=-1, verbose=0):
+             device=-1, verbose=0, radius_offset=0.0):
         o = cls()
         o.struct_size = ctypes.sizeof(cls)
         o.num_indexed_dims = int(num_indexed_dims or 0)
@@ -57,7 +58,23 @@ class Options(ctypes.Structure):
         o.max_iterations = int(max_iterations)
         o.device = int(device)
         o.verbose = int(verbose)
+        o.radius_offset = float(radius_offset)
         return o
+
+
+class TrainOptions(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("epochs", ctypes.c_int32),
+        ("batch", ctypes.c_uint32),
+        ("lr", ctypes.c_float),
+        ("quantile", ctypes.c_float),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
+RADIUS_FEATURES = 24
+RADIUS_MODEL_FLOATS = 5873
 
 
 class Stats(ctypes.Structure):
@@ -142,6 +159,16 @@ _SIGNATURES = [
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ("knnsj_write_outlier_scores", ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint64, ctypes.c_uint32,
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    ("knnsj_get_radius_model", ctypes.c_int, [ctypes.c_void_p]),
+    ("knnsj_set_radius_model", ctypes.c_int, [ctypes.c_void_p]),
+    ("knnsj_radius_features", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint32,
+                                             ctypes.c_uint32, ctypes.POINTER(Options), ctypes.c_void_p,
+                                             ctypes.POINTER(ctypes.c_double)]),
+    ("knnsj_radius_predict", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]),
+    ("knnsj_radius_grad", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                         ctypes.c_float, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    ("knnsj_radius_train", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                          ctypes.POINTER(TrainOptions), ctypes.c_void_p, ctypes.c_void_p]),
 ]
 
 

@@ -3,10 +3,14 @@
 // staging and error translation live here; the join itself is run_join
 // (join.cu).
 
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #ifdef KNNSJ_BUILD_DTYPE_DOUBLE
 #define KNNSJ_KNNJOINPY_DOUBLE 1
@@ -49,7 +53,10 @@ knnsj_status make_config(const knnsj_options* o, uint32_t d, JoinConfig* c) {
     c->radius_mode = o->radius_mode;
     c->max_iterations = o->max_iterations;
     if (o->verbose) c->verbose = o->verbose;
+    if (o->struct_size >= offsetof(knnsj_options, radius_offset) + sizeof(double))
+      c->radius_offset = o->radius_offset;
   }
+  if (const char* e = env("KNNSJ_RADIUS_MODE")) c->radius_mode = std::atoi(e);
   if (c->num_indexed_dims == 0 || c->num_indexed_dims > d) c->num_indexed_dims = d < 6 ? d : 6;
   if (c->num_indexed_dims > (uint32_t)MAX_DI) return KNNSJ_ERR_UNSUPPORTED;
   if (!(c->beta >= 0.0) || !(c->beta <= 1.0)) return KNNSJ_ERR_INVALID_ARGUMENT;
@@ -275,6 +282,129 @@ knnsj_status knnsj_selfjoin_batched(uint32_t n_sets, knnsj_set* sets, knnsj_dtyp
     *stats = agg;
   }
   return first;
+}
+
+knnsj_status knnsj_get_radius_model(float* out) {
+  if (!out) return KNNSJ_ERR_INVALID_ARGUMENT;
+  std::vector<float> m;
+  radius_model_snapshot(&m);
+  std::memcpy(out, m.data(), m.size() * sizeof(float));
+  return KNNSJ_OK;
+}
+
+knnsj_status knnsj_set_radius_model(const float* model) {
+  if (model)
+    for (int i = 0; i < KNNSJ_RADIUS_MODEL_FLOATS; i++)
+      if (!std::isfinite(model[i])) return KNNSJ_ERR_INVALID_ARGUMENT;
+  radius_model_set(model);
+  return KNNSJ_OK;
+}
+
+knnsj_status knnsj_radius_features(const void* data, knnsj_dtype dtype, uint64_t n, uint32_t d, uint32_t k,
+                                   const knnsj_options* opts, float* out_features, double* out_eps0) {
+  knnsj_status v = validate(data, n, d, k, out_features, out_features);
+  if (v != KNNSJ_OK) return v;
+  JoinConfig cfg;
+  v = make_config(opts, d, &cfg);
+  if (v != KNNSJ_OK) return v;
+  std::lock_guard<std::mutex> lock(g_call_mutex);
+  return guarded(
+      [&] {
+        const int dev = select_device(opts);
+        Workspace& w = ready_workspace(dev);
+        cudaStream_t s = w.stream;
+        const size_t es = dtype == KNNSJ_F32 ? 4 : 8;
+        void* din = w.in.get(n * d * es);
+        float* dout = (float*)w.dists.get(n * KNNSJ_RADIUS_FEATURES * 4);
+        KNNSJ_CUDA(cudaMemcpyAsync(din, data, n * d * es, cudaMemcpyHostToDevice, s));
+        if (dtype == KNNSJ_F32)
+          run_features<float>(w, cfg, (const float*)din, (const float*)data, n, d, k, dout, out_eps0, s);
+        else
+          run_features<double>(w, cfg, (const double*)din, (const double*)data, n, d, k, dout, out_eps0, s);
+        KNNSJ_CUDA(cudaMemcpyAsync(out_features, dout, n * KNNSJ_RADIUS_FEATURES * 4, cudaMemcpyDeviceToHost, s));
+        KNNSJ_CUDA(cudaStreamSynchronize(s));
+      },
+      nullptr);
+}
+
+knnsj_status knnsj_radius_predict(const float* model, const float* features, uint64_t n, float* out) {
+  if (!model || !features || !out) return KNNSJ_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(g_call_mutex);
+  return guarded(
+      [&] {
+        const int dev = select_device(nullptr);
+        Workspace& w = ready_workspace(dev);
+        cudaStream_t s = w.stream;
+        float* dm = (float*)w.perm.get(KNNSJ_RADIUS_MODEL_FLOATS * 4);
+        float* df = (float*)w.in.get(std::max<uint64_t>(n, 1) * KNNSJ_RADIUS_FEATURES * 4);
+        float* dy = (float*)w.dists.get(std::max<uint64_t>(n, 1) * 4);
+        KNNSJ_CUDA(cudaMemcpyAsync(dm, model, KNNSJ_RADIUS_MODEL_FLOATS * 4, cudaMemcpyHostToDevice, s));
+        KNNSJ_CUDA(cudaMemcpyAsync(df, features, n * KNNSJ_RADIUS_FEATURES * 4, cudaMemcpyHostToDevice, s));
+        launch_mlp_predict(dm, df, n, dy, s);
+        KNNSJ_CUDA(cudaMemcpyAsync(out, dy, n * 4, cudaMemcpyDeviceToHost, s));
+        KNNSJ_CUDA(cudaStreamSynchronize(s));
+      },
+      nullptr);
+}
+
+knnsj_status knnsj_radius_grad(const float* model, const float* features, const float* targets, uint64_t n,
+                               float quantile, float* out_grad, double* out_loss) {
+  if (!model || !features || !targets || !out_grad || n == 0 || !(quantile > 0.0f && quantile < 1.0f))
+    return KNNSJ_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(g_call_mutex);
+  return guarded(
+      [&] {
+        const int dev = select_device(nullptr);
+        Workspace& w = ready_workspace(dev);
+        cudaStream_t s = w.stream;
+        float* dm = (float*)w.perm.get(KNNSJ_RADIUS_MODEL_FLOATS * 4);
+        float* df = (float*)w.in.get(n * KNNSJ_RADIUS_FEATURES * 4);
+        float* dt = (float*)w.ids.get(n * 4);
+        const size_t np = mlp_grad_partials(n);
+        float* dpart = (float*)w.dists.get(np * 4);
+        double* dpl = (double*)w.eps_partial.get(((n + 63) / 64) * 8);
+        float* dg = (float*)w.eps_sample.get(KNNSJ_RADIUS_MODEL_FLOATS * 4);
+        KNNSJ_CUDA(cudaMemcpyAsync(dm, model, KNNSJ_RADIUS_MODEL_FLOATS * 4, cudaMemcpyHostToDevice, s));
+        KNNSJ_CUDA(cudaMemcpyAsync(df, features, n * KNNSJ_RADIUS_FEATURES * 4, cudaMemcpyHostToDevice, s));
+        KNNSJ_CUDA(cudaMemcpyAsync(dt, targets, n * 4, cudaMemcpyHostToDevice, s));
+        mlp_grad_device(dm, df, dt, nullptr, n, quantile, 1.0f / (float)n, dpart, dpl, dg, s);
+        const size_t ntrain = KNNSJ_RADIUS_MODEL_FLOATS - 2 * KNNSJ_RADIUS_FEATURES;
+        KNNSJ_CUDA(cudaMemcpyAsync(out_grad, dg, ntrain * 4, cudaMemcpyDeviceToHost, s));
+        std::vector<double> pl((n + 63) / 64);
+        KNNSJ_CUDA(cudaMemcpyAsync(pl.data(), dpl, pl.size() * 8, cudaMemcpyDeviceToHost, s));
+        KNNSJ_CUDA(cudaStreamSynchronize(s));
+        if (out_loss) {
+          double l = 0.0;
+          for (double x : pl) l += x;
+          *out_loss = l / (double)n;
+        }
+      },
+      nullptr);
+}
+
+knnsj_status knnsj_radius_train(const float* features, const float* targets, uint64_t n,
+                                const knnsj_train_options* o, float* model_out, float* loss_per_epoch) {
+  if (!features || !targets || !model_out || n == 0) return KNNSJ_ERR_INVALID_ARGUMENT;
+  int epochs = 8;
+  uint32_t batch = 8192;
+  float lr = 1e-3f, quantile = 0.9f;
+  uint64_t seed = 1;
+  if (o) {
+    if (o->epochs > 0) epochs = o->epochs;
+    if (o->batch > 0) batch = o->batch;
+    if (o->lr > 0) lr = o->lr;
+    if (o->quantile > 0) quantile = o->quantile;
+    seed = o->seed;
+  }
+  if (!(quantile > 0.0f && quantile < 1.0f)) return KNNSJ_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(g_call_mutex);
+  return guarded(
+      [&] {
+        const int dev = select_device(nullptr);
+        Workspace& w = ready_workspace(dev);
+        train_model(features, targets, n, epochs, batch, lr, quantile, seed, model_out, loss_per_epoch, w.stream);
+      },
+      nullptr);
 }
 
 void knnsj_release(void) {

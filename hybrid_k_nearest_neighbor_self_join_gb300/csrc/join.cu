@@ -28,6 +28,7 @@
 
 #include "knnsj_internal.h"
 #include "knnsj_host.h"
+#include "radius_model.cuh"
 
 namespace knnsj {
 
@@ -66,7 +67,8 @@ Workspace& workspace(int device) {
 }
 
 void Workspace::release_all() {
-  DevBuf* bufs[] = {&in, &ids, &dists, &xs, &ps, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
+  model_version = 0;
+  DevBuf* bufs[] = {&model, &in, &ids, &dists, &xs, &ps, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
                     &scan_tmp, &flags, &pos, &ckeys, &coff, &dstart, &list0, &list1, &small,
                     &eps_partial, &eps_sample, &perm, &minmax_part, &qradius};
   for (DevBuf* b : bufs) b->release();
@@ -113,6 +115,7 @@ struct SmallDev {  // layout of Workspace::small
   uint32_t hist[10000];
   double csum;
   double cpart[1024];
+  unsigned long long rmax_bits;
 };
 
 template <typename T>
@@ -203,14 +206,23 @@ static double ring_rows(double r, double w, uint32_t di) {
   return std::pow(per, (double)(di > 0 ? di - 1 : 0));
 }
 
+// Steps 1-4 of the pipeline: dimension order, column transpose, eps0 and
+// the grid index at eps0.
 template <typename T>
-void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
-              uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s) {
+struct Prepared {
+  DeviceGrid<T> grid;
+  T* xs = nullptr;
+  T eps0 = 0;
+  int bucket = -1;
+  double avg = 0.0;
+  std::vector<T> mn, mx;
+};
+
+template <typename T>
+static void prepare(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
+                    uint32_t k, knnsj_stats* st, cudaStream_t s, Prepared<T>* P) {
   const uint32_t K = k + 1;
   const uint32_t di = cfg.num_indexed_dims;
-  cudaEvent_t* ev = w.ev;
-  g_launches = 0;
-  KNNSJ_CUDA(cudaEventRecord(ev[0], s));
 
   // 1. dimension order
   std::vector<uint32_t> perm(d);
@@ -279,18 +291,23 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     ec = choose_eps(hh.data(), 10000, head.avg[0], n, k, cfg.beta);
   }
   T eps0 = (T)ec.eps;
-  std::vector<T> mn(di), mx(di);
+  P->mn.assign(di, 0);
+  P->mx.assign(di, 0);
   for (uint32_t j = 0; j < di; j++) {
-    mn[j] = hmm[2 * j];
-    mx[j] = hmm[2 * j + 1];
+    P->mn[j] = hmm[2 * j];
+    P->mx[j] = hmm[2 * j + 1];
   }
   int bucket = ec.bucket;
   if (!(eps0 > 0) || !std::isfinite((double)eps0)) {
     // The reference divides by a zero epsilon here (N <= 1000 gives a zero
     // sampled mean); any positive width keeps the join exact.
-    eps0 = host_fallback_eps<T>(mn, mx, n, K);
+    eps0 = host_fallback_eps<T>(P->mn, P->mx, n, K);
     bucket = -1;
   }
+  P->eps0 = eps0;
+  P->bucket = bucket;
+  P->avg = head.avg[0];
+  P->xs = xs;
   if (st) {
     st->eps0 = (double)eps0;
     st->eps_bucket = bucket;
@@ -298,16 +315,65 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   }
 
   // 4. grid at eps0
-  DeviceGrid<T> grid;
-  build_grid<T>(w, cfg, n, d, di, mn, mx, eps0, &grid, s);
-  if (st) st->nonempty_cells = grid.C;
+  build_grid<T>(w, cfg, n, d, di, P->mn, P->mx, eps0, &P->grid, s);
+  if (st) st->nonempty_cells = P->grid.C;
+}
+
+// The radius model used by the learned starting radius, uploaded to the
+// device when it changed since the last call.
+static const float* device_model(Workspace& w, cudaStream_t s) {
+  std::vector<float> m;
+  const unsigned v = radius_model_snapshot(&m);
+  float* dm = (float*)w.model.get(MODEL_FLOATS * 4);
+  if (w.model_version != v) {
+    KNNSJ_CUDA(cudaMemcpyAsync(dm, m.data(), MODEL_FLOATS * 4, cudaMemcpyHostToDevice, s));
+    KNNSJ_CUDA(cudaStreamSynchronize(s));
+    w.model_version = v;
+  }
+  return dm;
+}
+
+template <typename T>
+static double decode_radius(unsigned long long bits) {
+  if (sizeof(T) == 4) {
+    const uint32_t b = (uint32_t)bits;
+    float f;
+    std::memcpy(&f, &b, 4);
+    return (double)f;
+  }
+  double x;
+  std::memcpy(&x, &bits, 8);
+  return x;
+}
+
+template <typename T>
+void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
+              uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s) {
+  const uint32_t K = k + 1;
+  const uint32_t di = cfg.num_indexed_dims;
+  cudaEvent_t* ev = w.ev;
+  g_launches = 0;
+  KNNSJ_CUDA(cudaEventRecord(ev[0], s));
+  Prepared<T> P;
+  prepare<T>(w, cfg, d_aos, h_aos, n, d, k, st, s, &P);
+  SmallDev* sm = (SmallDev*)w.small.p;
   KNNSJ_CUDA(cudaEventRecord(ev[1], s));
 
-  // 5. retry loop
+  // 5. starting radii: eps0 for every query (plain), or one per query
+  T* qrad = nullptr;
+  double rmax = (double)P.eps0;
+  if (cfg.radius_mode == KNNSJ_RADIUS_LEARNED) {
+    qrad = (T*)w.qradius.get(n * sizeof(T));
+    launch_radius_assign<T>(P.grid, n, d, k, (float)cfg.beta, device_model(w, s), (double)P.eps0,
+                            (float)cfg.radius_offset, qrad, s);
+    rmax = (double)P.eps0 * learned_max_cells(di);
+  }
+
+  // 6. retry loop (main.cu:312-430)
   uint32_t* list[2] = {(uint32_t*)w.list0.get(n * 4), (uint32_t*)w.list1.get(n * 4)};
   SearchLaunch<T> a;
-  a.grid = grid;
-  a.xs = xs;
+  a.grid = P.grid;
+  a.xs = P.xs;
   a.n = n;
   a.d = d;
   a.K = K;
@@ -316,22 +382,25 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   a.fail_count = &sm->fail_count;
   a.cand_count = &sm->cand;
   a.work_counter = &sm->work_counter;
-  T r = eps0;
-  const double step = (double)eps0 * 0.5;
+  a.rmax_bits = &sm->rmax_bits;
+  a.qradius = qrad;
+  T r = P.eps0;
+  const double step = (double)P.eps0 * 0.5;
+  a.step = (T)step;
   uint32_t nq = (uint32_t)n;
   int iter = 0, regrids = 0, cur = 0;
   uint64_t queries_run = 0;
-  double kernel_ms = 0.0, alg_bytes = 0.0;
+  double kernel_ms = 0.0, alg_bytes = 0.0, rmax_seen = rmax;
   const int max_iter = cfg.max_iterations > 0 ? cfg.max_iterations : 100000;
   while (nq > 0) {
     if (iter >= max_iter) throw StatusError{KNNSJ_ERR_NO_CONVERGENCE, "iteration cap reached"};
-    const double rows = ring_rows((double)r, (double)a.grid.geom.width, di);
+    const double rows = ring_rows(rmax, (double)a.grid.geom.width, di);
     const double allowed = std::max(std::pow(3.0, (double)(di - 1)), 64.0);
-    if (rows > allowed && (double)r > (double)a.grid.geom.width) {
-      // coarser grid at the current radius (like main.cu:333-356); the
-      // widened width keeps the ring at three cells per dimension
-      const T wnew = (T)((double)r * (1.0 + 1.0 / 32768.0));
-      build_grid<T>(w, cfg, n, d, di, mn, mx, wnew, &a.grid, s);
+    if (rows > allowed && rmax > (double)a.grid.geom.width) {
+      // coarser grid for the largest radius in flight (like main.cu:333-356);
+      // the widened width keeps its ring at three cells per dimension
+      const T wnew = (T)(rmax * (1.0 + 1.0 / 32768.0));
+      build_grid<T>(w, cfg, n, d, di, P.mn, P.mx, wnew, &a.grid, s);
       regrids++;
     }
     a.qlist = iter == 0 ? nullptr : list[cur];
@@ -339,12 +408,19 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     a.radius = r;
     a.fail_list = list[cur ^ 1];
     KNNSJ_CUDA(cudaMemsetAsync(&sm->fail_count, 0, 4, s));
+    KNNSJ_CUDA(cudaMemsetAsync(&sm->rmax_bits, 0, 8, s));
     KNNSJ_CUDA(cudaEventRecord(ev[4], s));
     launch_search<T>(a, w.sm_count, s);
     KNNSJ_CUDA(cudaEventRecord(ev[5], s));
-    uint32_t nfail = 0;
-    KNNSJ_CUDA(cudaMemcpyAsync(&nfail, &sm->fail_count, 4, cudaMemcpyDeviceToHost, s));
+    struct {
+      uint32_t fail;
+      uint32_t pad;
+      unsigned long long rbits;
+    } tail;
+    KNNSJ_CUDA(cudaMemcpyAsync(&tail.fail, &sm->fail_count, 4, cudaMemcpyDeviceToHost, s));
+    KNNSJ_CUDA(cudaMemcpyAsync(&tail.rbits, &sm->rmax_bits, 8, cudaMemcpyDeviceToHost, s));
     KNNSJ_CUDA(cudaStreamSynchronize(s));
+    const uint32_t nfail = tail.fail;
     float kms = 0.f;
     KNNSJ_CUDA(cudaEventElapsedTime(&kms, ev[4], ev[5]));
     kernel_ms += kms;
@@ -355,7 +431,15 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     nq = nfail;
     cur ^= 1;
     iter++;
-    if (nq > 0) r = (T)((double)r + step);  // main.cu:336
+    if (nq > 0) {
+      if (qrad) {
+        rmax = decode_radius<T>(tail.rbits);  // largest grown radius among the failures
+      } else {
+        r = (T)((double)r + step);  // main.cu:336
+        rmax = (double)r;
+      }
+      rmax_seen = std::max(rmax_seen, rmax);
+    }
   }
   KNNSJ_CUDA(cudaEventRecord(ev[2], s));
   unsigned long long cand = 0;
@@ -364,7 +448,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   if (st) {
     st->iterations = iter;
     st->regrids = regrids;
-    st->eps_final = (double)r;
+    st->eps_final = qrad ? rmax_seen : (double)r;
     st->candidates = cand;
     st->queries_run = queries_run;
     st->kernel_launches = g_launches;
@@ -378,6 +462,19 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     st->ms_search = a12;
     st->ms_total = a01 + a12;
   }
+}
+
+// Features of the learned starting radius for every point (by input row),
+// on the eps0 grid of a (plain) join of the same data and k.
+template <typename T>
+void run_features(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
+                  uint32_t k, float* d_out, double* eps0_out, cudaStream_t s) {
+  g_launches = 0;
+  Prepared<T> P;
+  prepare<T>(w, cfg, d_aos, h_aos, n, d, k, nullptr, s, &P);
+  launch_radius_features<T>(P.grid, n, d, k, (float)cfg.beta, d_out, s);
+  KNNSJ_CUDA(cudaStreamSynchronize(s));
+  if (eps0_out) *eps0_out = (double)P.eps0;
 }
 
 template <typename T>
@@ -396,5 +493,9 @@ template void run_join<float>(Workspace&, const JoinConfig&, const float*, const
                               uint32_t, int32_t*, float*, knnsj_stats*, cudaStream_t);
 template void run_join<double>(Workspace&, const JoinConfig&, const double*, const double*, uint64_t,
                                uint32_t, uint32_t, int32_t*, double*, knnsj_stats*, cudaStream_t);
+template void run_features<float>(Workspace&, const JoinConfig&, const float*, const float*, uint64_t, uint32_t,
+                                  uint32_t, float*, double*, cudaStream_t);
+template void run_features<double>(Workspace&, const JoinConfig&, const double*, const double*, uint64_t,
+                                   uint32_t, uint32_t, float*, double*, cudaStream_t);
 
 }  // namespace knnsj

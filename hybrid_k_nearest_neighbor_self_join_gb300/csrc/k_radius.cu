@@ -1,0 +1,158 @@
+// k_radius.cu -- radius assignment for the learned starting radius: the
+// features of radius_model.cuh and the MLP evaluated in one pass, one thread
+// per query, queries in cell order (neighbouring threads read neighbouring
+// points and the same cell-table entries).  The model lives in shared memory.
+
+#include <cmath>
+#include <mutex>
+#include <vector>
+
+#include "knnsj_internal.h"
+#include "radius_model.cuh"
+
+namespace knnsj {
+
+// kRadiusModelDefault[MODEL_FLOATS]: the model trained by
+// hybrid_k_nearest_neighbor_self_join_gb300/train_radius.py.
+#include "radius_model_weights.inc"
+
+namespace {
+std::mutex g_model_mu;
+std::vector<float> g_model;
+unsigned g_model_version = 0;
+}  // namespace
+
+unsigned radius_model_snapshot(std::vector<float>* out) {
+  std::lock_guard<std::mutex> lock(g_model_mu);
+  if (g_model.empty()) {
+    g_model.assign(kRadiusModelDefault, kRadiusModelDefault + MODEL_FLOATS);
+    g_model_version = 1;
+  }
+  *out = g_model;
+  return g_model_version;
+}
+
+void radius_model_set(const float* model) {
+  std::lock_guard<std::mutex> lock(g_model_mu);
+  if (model)
+    g_model.assign(model, model + MODEL_FLOATS);
+  else
+    g_model.assign(kRadiusModelDefault, kRadiusModelDefault + MODEL_FLOATS);
+  g_model_version = g_model_version + 1 == 0 ? 1 : g_model_version + 1;
+}
+
+namespace {
+
+constexpr int RA_THREADS = 128;
+
+template <typename T>
+CellTable<T> table_of(const DeviceGrid<T>& g) {
+  CellTable<T> t;
+  t.g = g.geom;
+  t.ckeys = g.ckeys;
+  t.coff = g.coff;
+  t.dstart = g.dstart;
+  t.C = g.C;
+  t.dense = g.dense;
+  return t;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RA_THREADS) radius_assign_kernel(const CellTable<T> t, const T* __restrict__ ps,
+                                                                   const uint32_t* __restrict__ pid, uint64_t n,
+                                                                   uint32_t d, uint32_t k, float beta,
+                                                                   const float* __restrict__ model, float eps0f,
+                                                                   float log_lo, float log_hi, float offset,
+                                                                   T* __restrict__ qradius) {
+  __shared__ float sm[MODEL_FLOATS];
+  for (int i = threadIdx.x; i < MODEL_FLOATS; i += blockDim.x) sm[i] = model[i];
+  __syncthreads();
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T q[MAX_DI];
+  for (uint32_t j = 0; j < t.g.di; j++) q[j] = ps[(uint64_t)j * n + i];
+  float f[NFEAT];
+  radius_features(t, q, d, k, beta, n, f);
+  float y = mlp_eval(sm, f) + offset;
+  y = fminf(fmaxf(y, log_lo), log_hi);
+  qradius[pid[i]] = (T)(eps0f * expf(y));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RA_THREADS) radius_features_kernel(const CellTable<T> t, const T* __restrict__ ps,
+                                                                     const uint32_t* __restrict__ pid, uint64_t n,
+                                                                     uint32_t d, uint32_t k, float beta,
+                                                                     float* __restrict__ out) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T q[MAX_DI];
+  for (uint32_t j = 0; j < t.g.di; j++) q[j] = ps[(uint64_t)j * n + i];
+  float f[NFEAT];
+  radius_features(t, q, d, k, beta, n, f);
+  float* o = out + (uint64_t)pid[i] * NFEAT;
+  for (int j = 0; j < NFEAT; j++) o[j] = f[j];
+}
+
+__global__ void __launch_bounds__(RA_THREADS) mlp_predict_kernel(const float* __restrict__ model,
+                                                                 const float* __restrict__ feat, uint64_t n,
+                                                                 float* __restrict__ out) {
+  __shared__ float sm[MODEL_FLOATS];
+  for (int i = threadIdx.x; i < MODEL_FLOATS; i += blockDim.x) sm[i] = model[i];
+  __syncthreads();
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float f[NFEAT];
+  for (int j = 0; j < NFEAT; j++) f[j] = feat[i * NFEAT + j];
+  out[i] = mlp_eval(sm, f);
+}
+
+}  // namespace
+
+// Largest ring half-width (in cells of the eps0 grid) a learned radius may
+// start with: keeps a ring at most ~1024 rows; growth beyond is handled by
+// the retry schedule and grid rebuilds.
+double learned_max_cells(uint32_t di) {
+  switch (di) {
+    case 1: return 64.0;
+    case 2: return 64.0;
+    case 3: return 15.0;
+    case 4: return 4.0;
+    case 5: return 2.0;
+    default: return 1.0;
+  }
+}
+
+template <typename T>
+void launch_radius_assign(const DeviceGrid<T>& g, uint64_t n, uint32_t d, uint32_t k, float beta,
+                          const float* d_model, double eps0, float offset, T* qradius, cudaStream_t s) {
+  const float log_lo = std::log(1.0f / 16.0f);
+  const float log_hi = (float)std::log(learned_max_cells(g.geom.di) * (1.0 - 1.0 / 4096.0));
+  radius_assign_kernel<T><<<(unsigned)((n + RA_THREADS - 1) / RA_THREADS), RA_THREADS, 0, s>>>(
+      table_of(g), g.ps, g.pid, n, d, k, beta, d_model, (float)eps0, log_lo, log_hi, offset, qradius);
+  KNNSJ_CHECK_LAUNCH();
+}
+
+template <typename T>
+void launch_radius_features(const DeviceGrid<T>& g, uint64_t n, uint32_t d, uint32_t k, float beta, float* out,
+                            cudaStream_t s) {
+  radius_features_kernel<T><<<(unsigned)((n + RA_THREADS - 1) / RA_THREADS), RA_THREADS, 0, s>>>(
+      table_of(g), g.ps, g.pid, n, d, k, beta, out);
+  KNNSJ_CHECK_LAUNCH();
+}
+
+void launch_mlp_predict(const float* d_model, const float* d_feat, uint64_t n, float* d_out, cudaStream_t s) {
+  if (n == 0) return;
+  mlp_predict_kernel<<<(unsigned)((n + RA_THREADS - 1) / RA_THREADS), RA_THREADS, 0, s>>>(d_model, d_feat, n, d_out);
+  KNNSJ_CHECK_LAUNCH();
+}
+
+template void launch_radius_assign<float>(const DeviceGrid<float>&, uint64_t, uint32_t, uint32_t, float,
+                                          const float*, double, float, float*, cudaStream_t);
+template void launch_radius_assign<double>(const DeviceGrid<double>&, uint64_t, uint32_t, uint32_t, float,
+                                           const float*, double, float, double*, cudaStream_t);
+template void launch_radius_features<float>(const DeviceGrid<float>&, uint64_t, uint32_t, uint32_t, float, float*,
+                                            cudaStream_t);
+template void launch_radius_features<double>(const DeviceGrid<double>&, uint64_t, uint32_t, uint32_t, float, float*,
+                                             cudaStream_t);
+
+}  // namespace knnsj

@@ -83,6 +83,7 @@ struct SearchParams {
   uint32_t* fail_count;
   unsigned long long* cand_count;
   uint32_t* work_counter;
+  unsigned long long* rmax_bits;
 };
 
 __device__ __forceinline__ unsigned long long lower_bound_u64(const unsigned long long* __restrict__ a,
@@ -651,7 +652,12 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
       } else if (lane == 0) {
         const uint32_t slot = atomicAdd(p.fail_count, 1u);
         p.fail_list[slot] = qid;
-        if (p.qradius) p.qradius[qid] = (T)((double)r + p.step);
+        if (p.qradius) {
+          // the plain BETA schedule from the learned start: grow by eps0/2
+          const T rn = (T)((double)r + p.step);
+          p.qradius[qid] = rn;
+          atomicMax(p.rmax_bits, (unsigned long long)Num<T>::bits(rn));
+        }
       }
       __syncwarp();
     }
@@ -719,6 +725,7 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s) {
   p.fail_count = a.fail_count;
   p.cand_count = a.cand_count;
   p.work_counter = a.work_counter;
+  p.rmax_bits = a.rmax_bits;
   KNNSJ_CUDA(cudaMemsetAsync(a.work_counter, 0, sizeof(uint32_t), s));
   const bool full = a.grid.geom.di == a.d;  // every dimension indexed
   switch (a.d) {

@@ -24,6 +24,7 @@ struct JoinConfig {
   int max_iterations = 0;
   int verbose = 0;
   int dense_mode = 1;  // 0 never, 1 auto, 2 always (testing)
+  double radius_offset = 0.0;  // added to the learned log-radius
 };
 
 // ReorderByDimension (main.cu:2521-2615).  `sample` holds rows 0, 100, 200,

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cuda_runtime.h>
+#include <vector>
 
 #include "../../include/knnsj.h"
 #include "knnsj_device.cuh"
@@ -134,6 +135,7 @@ struct SearchLaunch {
   uint32_t* fail_count = nullptr;
   unsigned long long* cand_count = nullptr;
   uint32_t* work_counter = nullptr;
+  unsigned long long* rmax_bits = nullptr;  // largest grown radius of a failure (per-query radii)
 };
 template <typename T>
 void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s);
@@ -141,6 +143,8 @@ int search_buffer_capacity(uint32_t K);
 
 // ---- per-device workspace --------------------------------------------------
 struct Workspace {
+  DevBuf model;                          // radius model (learned starting radius)
+  unsigned model_version = 0;
   DevBuf in, ids, dists;                 // staging for host-pointer calls
   DevBuf xs, ps, pid;                    // input-order columns, cell-order columns, ids
   DevBuf keys0, keys1, vals0, vals1, hist, scan_tmp, flags, pos;  // grid build
@@ -164,6 +168,29 @@ struct JoinConfig;
 template <typename T>
 void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
               uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s);
+template <typename T>
+void run_features(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
+                  uint32_t k, float* d_out, double* eps0_out, cudaStream_t s);
+
+// ---- learned starting radius (k_radius.cu, k_mlp.cu) -----------------------
+double learned_max_cells(uint32_t di);
+template <typename T>
+void launch_radius_assign(const DeviceGrid<T>& g, uint64_t n, uint32_t d, uint32_t k, float beta,
+                          const float* d_model, double eps0, float offset, T* qradius, cudaStream_t s);
+template <typename T>
+void launch_radius_features(const DeviceGrid<T>& g, uint64_t n, uint32_t d, uint32_t k, float beta, float* out,
+                            cudaStream_t s);
+void launch_mlp_predict(const float* d_model, const float* d_feat, uint64_t n, float* d_out, cudaStream_t s);
+// Active model: a copy and its version (changes on every set).
+unsigned radius_model_snapshot(std::vector<float>* out);
+void radius_model_set(const float* model);  // nullptr restores the built-in model
+void mlp_grad_device(const float* d_model, const float* d_X, const float* d_Y, const uint32_t* d_idx, uint64_t n,
+                     float quantile, float inv_batch, float* d_part, double* d_part_loss, float* d_grad,
+                     cudaStream_t s);
+size_t mlp_grad_partials(uint64_t n);  // floats of d_part for n samples
+void train_model(const float* hX, const float* hY, uint64_t n, int epochs, uint32_t batch, float lr,
+                 float quantile, uint64_t seed, float* model_out, float* loss_out, cudaStream_t s);
+
 // Verification figure of a result table on the device (synchronises s).
 template <typename T>
 double device_checksum(Workspace& w, const T* d_vals, uint64_t count, cudaStream_t s);

@@ -72,6 +72,8 @@ typedef struct {
   int32_t max_iterations;   /* radius re-attempts cap; 0 -> automatic */
   int32_t device;           /* CUDA device ordinal; < 0 -> current device */
   int32_t verbose;          /* 1 prints phase timings on stderr [KNNSJ_VERBOSE] */
+  double radius_offset;     /* KNNSJ_RADIUS_LEARNED: added to the predicted
+                               log(radius / eps0); 0 = the model as trained */
   int32_t reserved[8];
 } knnsj_options;
 
@@ -162,6 +164,43 @@ knnsj_status knnsj_selfjoin_batched(uint32_t n_sets, knnsj_set* sets, knnsj_dtyp
 
 /* Frees the device workspace cached by previous calls on the current device. */
 void knnsj_release(void);
+
+/* ---- learned starting radius (no reference counterpart) ----
+ * A query's starting radius is eps0 * exp(MLP(features)), the MLP being
+ * 24 -> 64 -> 64 -> 1 (ReLU, FP32); features and model layout are defined in
+ * hybrid_k_nearest_neighbor_self_join_gb300/csrc/radius_model.cuh.  The
+ * acceptance rule is unchanged, so results do not depend on the model. */
+#define KNNSJ_RADIUS_FEATURES 24
+#define KNNSJ_RADIUS_MODEL_FLOATS 5873
+
+typedef struct {
+  uint32_t struct_size;
+  int32_t epochs;     /* passes over the samples (default 8) */
+  uint32_t batch;     /* samples per Adam step (default 8192) */
+  float lr;           /* Adam learning rate (default 1e-3) */
+  float quantile;     /* pinball-loss quantile of log(r_K/eps0) (default 0.9) */
+  uint64_t seed;      /* initialisation and shuffling seed */
+} knnsj_train_options;
+
+/* Copies the active model (KNNSJ_RADIUS_MODEL_FLOATS floats). */
+knnsj_status knnsj_get_radius_model(float* out);
+/* Replaces the active model; NULL restores the built-in one. */
+knnsj_status knnsj_set_radius_model(const float* model);
+/* Features of every point (row-major n x 24, by input row) on the eps0 grid
+ * of a join of (data, k) with opts; *out_eps0 receives eps0. */
+knnsj_status knnsj_radius_features(const void* data, knnsj_dtype dtype, uint64_t n, uint32_t d, uint32_t k,
+                                   const knnsj_options* opts, float* out_features, double* out_eps0);
+/* Model output for n feature rows (GPU). */
+knnsj_status knnsj_radius_predict(const float* model, const float* features, uint64_t n, float* out);
+/* Gradient of the mean pinball loss at `quantile` with respect to the
+ * trainable parameters (the model from offset 48 on: 5825 floats) and the
+ * loss itself, on n samples (GPU, deterministic). */
+knnsj_status knnsj_radius_grad(const float* model, const float* features, const float* targets, uint64_t n,
+                               float quantile, float* out_grad, double* out_loss);
+/* Trains a model on (features, targets = log(r_K / eps0)) with Adam on the
+ * GPU; loss_per_epoch (optional) receives the mean training loss per epoch. */
+knnsj_status knnsj_radius_train(const float* features, const float* targets, uint64_t n,
+                                const knnsj_train_options* opts, float* model_out, float* loss_per_epoch);
 
 /* ---- host-side pieces of the reference pipeline (no GPU needed) ---- */
 
