@@ -396,7 +396,10 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     if (iter >= max_iter) throw StatusError{KNNSJ_ERR_NO_CONVERGENCE, "iteration cap reached"};
     const double rows = ring_rows(rmax, (double)a.grid.geom.width, di);
     const double allowed = std::max(std::pow(3.0, (double)(di - 1)), 64.0);
-    if (rows > allowed && rmax > (double)a.grid.geom.width) {
+    // learned starting radii are clamped so their rings stay small on the
+    // eps0 grid: no rebuild for the first pass
+    const bool first_learned = qrad && iter == 0;
+    if (!first_learned && rows > allowed && rmax > (double)a.grid.geom.width) {
       // coarser grid for the largest radius in flight (like main.cu:333-356);
       // the widened width keeps its ring at three cells per dimension
       const T wnew = (T)(rmax * (1.0 + 1.0 / 32768.0));
