@@ -118,6 +118,7 @@ double learned_max_cells(uint32_t di) {
     case 3: return 15.0;
     case 4: return 4.0;
     case 5: return 2.0;
+    case 6: return 1.5;
     default: return 1.0;
   }
 }

@@ -19,7 +19,7 @@
 //   6      d / 8          7  log(k)        8  NUMINDEXEDDIM / 8    9  m / 2
 //   10..15 u_j - c_j - 1/2 for j < min(NUMINDEXEDDIM, 6), else 0
 //   16..21 u_j/2 - (c_j >> 1) - 1/2 for j < min(NUMINDEXEDDIM, 6), else 0
-//   22     BETA           23 log(N) / 16
+//   22     BETA           23 reserved, 0
 // Model (KNNSJ_MODEL_FLOATS floats): feature mean[24], feature 1/std[24],
 // W1[24][64], b1[64], W2[64][64], b2[64], W3[64], b3; ReLU after layers 1
 // and 2.  Output y estimates a high quantile of log(r_K / eps0), r_K being
@@ -140,7 +140,8 @@ __device__ void radius_features(const CellTable<T>& t, const T* q, uint32_t d, u
     f[16 + j] = b;
   }
   f[22] = beta;
-  f[23] = logf((float)n) / 16.0f;
+  f[23] = 0.0f;  // reserved (kept 0 so models stay independent of N)
+  (void)n;
 }
 
 // Model output for one feature vector (one thread).  model may live in

@@ -33,14 +33,16 @@ BETAS = (0.0, 0.025, 0.05)
 
 
 def training_sets(n_sets: int, n: int, seed: int):
-    """Seeded sets: d in 2..6, half uniform-heavy, half clustered."""
+    """Seeded sets: d in 2..6, uniform-heavy to clustered, sizes log-uniform
+    in [n/5, 2n]."""
     rng = np.random.default_rng(seed)
     for i in range(n_sets):
         d = int(rng.integers(2, 7))
         comps = int(rng.integers(1, 60))
         ufrac = float(rng.choice([0.05, 0.2, 0.5, 1.0]))
         sd_hi = float(rng.choice([0.02, 0.05, 0.1]))
-        x = datasets.gmm(n, d, comps, ufrac, seed * 1000 + i, sd_lo=0.002, sd_hi=sd_hi, dtype=np.float32)
+        m = int(np.exp(rng.uniform(np.log(n / 5), np.log(2 * n))))
+        x = datasets.gmm(m, d, comps, ufrac, seed * 1000 + i, sd_lo=0.002, sd_hi=sd_hi, dtype=np.float32)
         yield i, x, float(rng.choice(BETAS))
 
 
