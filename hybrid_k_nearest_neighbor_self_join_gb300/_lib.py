@@ -23,6 +23,7 @@ STATUS_NAMES = {
     3: "KNNSJ_ERR_K_TOO_LARGE", 4: "KNNSJ_ERR_NONFINITE_INPUT", 5: "KNNSJ_ERR_TOO_MANY_POINTS",
     6: "KNNSJ_ERR_NO_CONVERGENCE", 7: "KNNSJ_ERR_CUDA", 8: "KNNSJ_ERR_OUT_OF_MEMORY",
     9: "KNNSJ_ERR_NO_DEVICE", 10: "KNNSJ_ERR_UNSUPPORTED", 11: "KNNSJ_ERR_IO",
+    12: "KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH",
 }
 
 
@@ -145,6 +146,9 @@ _SIGNATURES = [
     ("knnsj_selfjoin_device", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64,
                                              ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(Options),
                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    ("knnsj_selfjoin_device_noalloc", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64,
+                                                     ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(Options),
+                                                     ctypes.c_void_p, ctypes.c_void_p]),
     ("knnsj_selfjoin_batched", ctypes.c_int, [ctypes.c_uint32, ctypes.POINTER(Set), ctypes.c_int,
                                               ctypes.POINTER(Options), ctypes.POINTER(Stats)]),
     ("knnsj_release", None, []),

@@ -185,6 +185,55 @@ void device_join(const T* data, uint64_t n, uint32_t d, uint32_t k, const JoinCo
   KNNSJ_CUDA(cudaStreamSynchronize(w.stream));
 }
 
+// ---- fixed-scratch join (knnsj_selfjoin_device_noalloc) --------------------
+// For callers that may not allocate device memory: a join inside CUDA stream
+// capture (cudaMalloc is illegal there), runtimes whose allocator owns all of
+// device memory and forbids raw cudaMalloc/cudaFree, and hosts that size every
+// allocation before they start.  All scratch of such a join is carved from this
+// array; each device that loads the library holds it until the process exits.
+// In host code `g_fixed_scratch` only names the symbol: its device address
+// comes from cudaGetSymbolAddress, looked up once per device.
+static __device__ __align__(256) unsigned char g_fixed_scratch[KNNSJ_NOALLOC_SCRATCH_BYTES];
+
+struct FixedScratchDevice {
+  bool ready = false;
+  Arena arena;
+  Workspace w;  // never given a stream or events: works on the legacy stream
+};
+
+// Set-up on the current device `dev` (the first call there): symbol address and
+// SM count.  Neither allocates; both must run outside stream capture.
+FixedScratchDevice& fixed_scratch_device(int dev) {
+  static std::vector<FixedScratchDevice*> all;
+  if ((int)all.size() <= dev) all.resize(dev + 1, nullptr);
+  if (!all[dev]) all[dev] = new FixedScratchDevice();
+  FixedScratchDevice& f = *all[dev];
+  if (!f.ready) {
+    unsigned char* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_fixed_scratch);
+    if (e != cudaSuccess) throw CudaError{e, "cudaGetSymbolAddress(g_fixed_scratch)"};
+    KNNSJ_CUDA(cudaDeviceGetAttribute(&f.w.sm_count, cudaDevAttrMultiProcessorCount, dev));
+    f.arena.base = ptr;
+    f.arena.cap = KNNSJ_NOALLOC_SCRATCH_BYTES;
+    f.ready = true;
+  }
+  return f;
+}
+
+template <typename T>
+void fixed_scratch_join(const T* data, uint64_t n, uint32_t d, uint32_t k, JoinConfig cfg, int dev,
+                        int32_t* out_ids, T* out_d) {
+  FixedScratchDevice& f = fixed_scratch_device(dev);
+  // every buffer is carved afresh from the start of the array; the pipeline
+  // clears what must start at zero, so the previous call's contents do not matter
+  f.arena.used = 0;
+  f.w.attach_arena(&f.arena);
+  cfg.dense_cells_cap = 4ull * n;  // keeps the dense cell table within the array
+  const cudaStream_t s = 0;
+  run_join<T>(f.w, cfg, data, nullptr, n, d, k, out_ids, out_d, nullptr, s);
+  KNNSJ_CUDA(cudaStreamSynchronize(s));
+}
+
 }  // namespace
 
 extern "C" {
@@ -205,6 +254,8 @@ const char* knnsj_status_string(knnsj_status s) {
     case KNNSJ_ERR_NO_DEVICE: return "no CUDA device";
     case KNNSJ_ERR_UNSUPPORTED: return "unsupported configuration";
     case KNNSJ_ERR_IO: return "file I/O error";
+    case KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH:
+      return "problem exceeds the fixed scratch array (n <= 65536, d <= 8, k+1 <= 128)";
   }
   return "unknown status";
 }
@@ -254,6 +305,38 @@ knnsj_status knnsj_selfjoin_device(const void* d_data, knnsj_dtype dtype, uint64
                               stats);
       },
       stats);
+}
+
+// The device join without any allocation (declared in include/knnsj.h).  All
+// calls share one array; calls whose GPU work overlapped would race on it.
+// This one holds the library's call lock and returns only after its GPU work
+// is done, so calls through it follow one another.
+knnsj_status knnsj_selfjoin_device_noalloc(const void* d_data, knnsj_dtype dtype, uint64_t n, uint32_t d,
+                                           uint32_t k, const knnsj_options* opts, int32_t* d_out_ids,
+                                           void* d_out_dists) {
+  knnsj_status v = validate(d_data, n, d, k, d_out_ids, d_out_dists);
+  if (v != KNNSJ_OK) return v;
+  if (dtype != KNNSJ_F32 && dtype != KNNSJ_F64) return KNNSJ_ERR_INVALID_ARGUMENT;
+  if (n > KNNSJ_NOALLOC_MAX_POINTS || d > 8 || k + 1 > 128) {
+    if (std::getenv("KNNSJ_VERBOSE"))
+      fprintf(stderr, "knnsj: fixed-scratch join limited to n <= %u, d <= 8, k+1 <= 128\n",
+              KNNSJ_NOALLOC_MAX_POINTS);
+    return KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH;
+  }
+  JoinConfig cfg;
+  v = make_config(opts, d, &cfg);
+  if (v != KNNSJ_OK) return v;
+  std::lock_guard<std::mutex> lock(g_call_mutex);
+  return guarded(
+      [&] {
+        const int dev = select_device(opts);
+        if (dtype == KNNSJ_F32)
+          fixed_scratch_join<float>((const float*)d_data, n, d, k, cfg, dev, d_out_ids, (float*)d_out_dists);
+        else
+          fixed_scratch_join<double>((const double*)d_data, n, d, k, cfg, dev, d_out_ids,
+                                     (double*)d_out_dists);
+      },
+      nullptr);
 }
 
 knnsj_status knnsj_selfjoin_batched(uint32_t n_sets, knnsj_set* sets, knnsj_dtype dtype,

@@ -34,8 +34,35 @@ namespace knnsj {
 
 unsigned long long g_launches = 0;
 
+void* Arena::take(size_t bytes) {
+  const size_t at = (used + 255) & ~(size_t)255;
+  if (at + bytes > cap)
+    throw StatusError{KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH, "problem exceeds the fixed scratch array"};
+  used = at + bytes;
+  return base + at;
+}
+
+void Workspace::attach_arena(Arena* a) {
+  DevBuf* bufs[] = {&model, &in, &ids, &dists, &xs, &ps, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
+                    &scan_tmp, &flags, &pos, &ckeys, &coff, &dstart, &list0, &list1, &small,
+                    &eps_partial, &eps_sample, &perm, &minmax_part, &qradius};
+  for (DevBuf* b : bufs) {
+    b->arena = a;
+    b->p = nullptr;
+    b->bytes = 0;
+  }
+  model_version = 0;
+}
+
 void* DevBuf::get(size_t need) {
   if (need == 0) need = 16;
+  if (arena) {
+    if (need > bytes) {
+      p = arena->take(need);
+      bytes = need;
+    }
+    return p;
+  }
   if (need > bytes) {
     if (p) cudaFree(p);
     p = nullptr;
@@ -52,7 +79,7 @@ void* DevBuf::get(size_t need) {
 }
 
 void DevBuf::release() {
-  if (p) cudaFree(p);
+  if (p && !arena) cudaFree(p);
   p = nullptr;
   bytes = 0;
 }
@@ -189,7 +216,8 @@ static void build_grid(Workspace& w, const JoinConfig& cfg, uint64_t n, uint32_t
   out->ckeys = ckeys;
   out->coff = coff;
   out->C = C;
-  const unsigned long long dense_limit = std::max<unsigned long long>(4ull * n, 1ull << 24);
+  const unsigned long long dense_limit =
+      cfg.dense_cells_cap ? cfg.dense_cells_cap : std::max<unsigned long long>(4ull * n, 1ull << 24);
   out->dense = (cfg.dense_mode != 0) && (g.total_cells <= dense_limit) && g.total_cells < (1ull << 31);
   if (cfg.dense_mode == 2) out->dense = g.total_cells < (1ull << 31);
   out->dstart = nullptr;
@@ -352,12 +380,21 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   const uint32_t K = k + 1;
   const uint32_t di = cfg.num_indexed_dims;
   cudaEvent_t* ev = w.ev;
+  // a workspace without events (fixed-scratch calls) records no timings
+  auto rec = [&](int i) {
+    if (ev[i]) KNNSJ_CUDA(cudaEventRecord(ev[i], s));
+  };
+  auto elapsed = [&](int a, int b) -> float {
+    float ms = 0.f;
+    if (ev[a] && ev[b]) KNNSJ_CUDA(cudaEventElapsedTime(&ms, ev[a], ev[b]));
+    return ms;
+  };
   g_launches = 0;
-  KNNSJ_CUDA(cudaEventRecord(ev[0], s));
+  rec(0);
   Prepared<T> P;
   prepare<T>(w, cfg, d_aos, h_aos, n, d, k, st, s, &P);
   SmallDev* sm = (SmallDev*)w.small.p;
-  KNNSJ_CUDA(cudaEventRecord(ev[1], s));
+  rec(1);
 
   // 5. starting radii: eps0 for every query (plain), or one per query
   T* qrad = nullptr;
@@ -412,9 +449,9 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     a.fail_list = list[cur ^ 1];
     KNNSJ_CUDA(cudaMemsetAsync(&sm->fail_count, 0, 4, s));
     KNNSJ_CUDA(cudaMemsetAsync(&sm->rmax_bits, 0, 8, s));
-    KNNSJ_CUDA(cudaEventRecord(ev[4], s));
+    rec(4);
     launch_search<T>(a, w.sm_count, s);
-    KNNSJ_CUDA(cudaEventRecord(ev[5], s));
+    rec(5);
     struct {
       uint32_t fail;
       uint32_t pad;
@@ -424,9 +461,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     KNNSJ_CUDA(cudaMemcpyAsync(&tail.rbits, &sm->rmax_bits, 8, cudaMemcpyDeviceToHost, s));
     KNNSJ_CUDA(cudaStreamSynchronize(s));
     const uint32_t nfail = tail.fail;
-    float kms = 0.f;
-    KNNSJ_CUDA(cudaEventElapsedTime(&kms, ev[4], ev[5]));
-    kernel_ms += kms;
+    kernel_ms += elapsed(4, 5);
     // candidate columns read once, query rows read, accepted rows written
     alg_bytes += (double)n * d * sizeof(T) + (double)nq * d * sizeof(T) +
                  (double)(nq - nfail) * K * (4.0 + sizeof(T));
@@ -444,7 +479,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
       rmax_seen = std::max(rmax_seen, rmax);
     }
   }
-  KNNSJ_CUDA(cudaEventRecord(ev[2], s));
+  rec(2);
   unsigned long long cand = 0;
   KNNSJ_CUDA(cudaMemcpyAsync(&cand, &sm->cand, 8, cudaMemcpyDeviceToHost, s));
   KNNSJ_CUDA(cudaStreamSynchronize(s));
@@ -458,9 +493,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     st->ms_search_kernels = kernel_ms;
     st->search_alg_bytes = alg_bytes;
     st->search_alg_flops = 3.0 * d * (double)cand;
-    float a01 = 0, a12 = 0;
-    cudaEventElapsedTime(&a01, ev[0], ev[1]);
-    cudaEventElapsedTime(&a12, ev[1], ev[2]);
+    const float a01 = elapsed(0, 1), a12 = elapsed(1, 2);
     st->ms_prep = a01;
     st->ms_search = a12;
     st->ms_total = a01 + a12;

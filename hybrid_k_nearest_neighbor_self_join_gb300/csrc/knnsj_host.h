@@ -25,6 +25,7 @@ struct JoinConfig {
   int verbose = 0;
   int dense_mode = 1;  // 0 never, 1 auto, 2 always (testing)
   double radius_offset = 0.0;  // added to the learned log-radius
+  unsigned long long dense_cells_cap = 0;  // largest grid given a dense cell table; 0 = default
 };
 
 // ReorderByDimension (main.cu:2521-2615).  `sample` holds rows 0, 100, 200,

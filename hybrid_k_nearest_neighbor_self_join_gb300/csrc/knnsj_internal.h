@@ -39,10 +39,19 @@ extern unsigned long long g_launches;
   } while (0)
 
 // ---- device buffers of one join (cached across calls, grow-only) --------
+// A fixed device region carved out by bump allocation (no cudaMalloc).
+struct Arena {
+  unsigned char* base = nullptr;
+  size_t cap = 0;
+  size_t used = 0;
+  void* take(size_t bytes);  // 256-byte aligned; throws when the region is full
+};
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
-  void* get(size_t need);  // grows with cudaMalloc (contents not kept)
+  Arena* arena = nullptr;  // non-null: carve from the arena instead of cudaMalloc
+  void* get(size_t need);  // grows (contents not kept)
   void release();
 };
 
@@ -159,6 +168,7 @@ struct Workspace {
   void* pinned(size_t need);
   void pinned_release();
   void release_all();
+  void attach_arena(Arena* a);  // every buffer carves from `a` from now on
 };
 Workspace& workspace(int device);
 

@@ -47,7 +47,8 @@ typedef enum {
   KNNSJ_ERR_OUT_OF_MEMORY = 8,
   KNNSJ_ERR_NO_DEVICE = 9,
   KNNSJ_ERR_UNSUPPORTED = 10,     /* e.g. NUMINDEXEDDIM > 8, k+1 > 2048 */
-  KNNSJ_ERR_IO = 11               /* file could not be read or written */
+  KNNSJ_ERR_IO = 11,              /* file could not be read or written */
+  KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH = 12 /* knnsj_selfjoin_device_noalloc: problem too large */
 } knnsj_status;
 
 typedef enum { KNNSJ_F32 = 0, KNNSJ_F64 = 1 } knnsj_dtype;
@@ -154,6 +155,30 @@ knnsj_status knnsj_selfjoin(const void* data, knnsj_dtype dtype, uint64_t n, uin
 knnsj_status knnsj_selfjoin_device(const void* d_data, knnsj_dtype dtype, uint64_t n,
                                    uint32_t d, uint32_t k, const knnsj_options* opts,
                                    int32_t* d_out_ids, void* d_out_dists, knnsj_stats* stats);
+
+/* No counterpart in the reference.  The device-buffer self-join for callers
+ * that must not allocate GPU memory: code running inside CUDA stream capture
+ * (where cudaMalloc is not allowed), allocator-managed runtimes that forbid
+ * raw cudaMalloc/cudaFree, and hosts that fix every device allocation up
+ * front.  It calls no cudaMalloc, cudaFree, stream or event creation and no
+ * allocating library routine; all scratch comes from one static device array
+ * of KNNSJ_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds
+ * until the process exits.  Limits: n <= KNNSJ_NOALLOC_MAX_POINTS, d <= 8,
+ * k+1 <= 128; larger problems return KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH.
+ * The caller passes the input and output device buffers, as for
+ * knnsj_selfjoin_device, and gets the same results.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  The call runs on the legacy
+ * default stream and returns when the join is done.  Every call reuses the
+ * same array, which keeps the previous call's contents (the join clears what
+ * must start at zero); calls whose GPU work overlapped would race on it, so
+ * the library takes its call lock and finishes each call's GPU work before
+ * returning. */
+#define KNNSJ_NOALLOC_SCRATCH_BYTES (24u << 20)
+#define KNNSJ_NOALLOC_MAX_POINTS 65536u
+knnsj_status knnsj_selfjoin_device_noalloc(const void* d_data, knnsj_dtype dtype, uint64_t n, uint32_t d,
+                                           uint32_t k, const knnsj_options* opts, int32_t* d_out_ids,
+                                           void* d_out_dists);
 
 /* Many independent self-joins (host buffers), each with its own n, d, k and
  * results identical to a knnsj_selfjoin call on that set.  No reference
