@@ -4,11 +4,14 @@
 Workload (one "step"): the full self-join of the 25M-point 2-D float32
 sky-like dataset at k=64, BETA=0.025 (the configuration the reference's
 headline figure is quoted on, README.md:34-37, with a seeded synthetic
-stand-in for the Gaia DR2 file) -- reorder, eps0, grid build, and every
-search pass -- with the points resident in HBM and the N x (k+1) result
-table left in HBM.  value = queries/s over all ranks.  e2e = the same join
-through the host API (knnsj_selfjoin) from pinned host memory, host->device
-input copy and device->host result copy inside the timed region.
+stand-in for the Gaia DR2 file) -- reorder, eps0, grid build, starting radii
+and every search pass -- with the points resident in HBM and the N x (k+1)
+result table left in HBM.  value = queries/s over all ranks with the learned
+starting radius; the plain BETA schedule is timed on the same data beside it
+(plain_beta, learned_over_plain) and its table compared bit for bit
+(identical_to_plain).  e2e = the learned join through the host API
+(knnsj_selfjoin) from pinned host memory, host->device input copy and
+device->host result copy inside the timed region.
 
 The reference arm (--impl reference) times the CPU restatement of the
 reference's algorithm (oracle/) on the host cores, on a bounded sample.
@@ -209,48 +212,57 @@ def run_gb300(args):
     x, k, beta, di = make_workload()
     n, d = x.shape
     K = k + 1
-    # ---- device-resident join -------------------------------------------
+    # ---- device-resident joins -------------------------------------------
     tx = torch.from_numpy(x).cuda()
     tids = torch.empty((n, K), dtype=torch.int32, device="cuda")
     td = torch.empty((n, K), dtype=torch.float32, device="cuda")
 
-    def step():
+    def step(mode):
         return kj.selfjoin_device(tx.data_ptr(), np.float32, n, d, k, tids.data_ptr(), td.data_ptr(),
-                                  num_indexed_dims=di, beta=beta)
+                                  num_indexed_dims=di, beta=beta, radius_mode=mode)
 
-    st = None
-    for _ in range(args.warmup):
-        st = step()
-    torch.cuda.synchronize()
-    dist.barrier()
+    def timed(mode, steps, warmup):
+        for _ in range(warmup):
+            step(mode)
+        torch.cuda.synchronize()
+        dist.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        sts = [step(mode) for _ in range(steps)]
+        e1.record()
+        torch.cuda.synchronize()
+        dist.barrier()
+        return dist.max(e0.elapsed_time(e1)), sts
+
+    # the learned radius (the headline) first, then the plain BETA schedule
+    # (the comparison); both must leave the same table, checked bit for bit
     clocks = ClockSampler(local)
     clocks.start()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record()
-    launches = 0
-    kernel_ms, alg_bytes, iters = [], [], []
-    for _ in range(args.steps):
-        st = step()
-        launches += st["kernel_launches"]
-        kernel_ms.append(st["ms_search_kernels"])
-        alg_bytes.append(st["search_alg_bytes"])
-        iters.append(st["iterations"])
-    e1.record()
-    torch.cuda.synchronize()
-    dist.barrier()
+    t_ms, sts = timed(kj.RADIUS_LEARNED, args.steps, args.warmup)
     clk = clocks.stop()
-    t_ms = dist.max(e0.elapsed_time(e1))
+    ref_ids, ref_d = tids.clone(), td.clone()
+    tids.fill_(-1)
+    t_plain, st_plain = timed(kj.RADIUS_PLAIN, max(2, min(args.steps, 3)), 1)
+    identical = bool(torch.equal(tids, ref_ids) and torch.equal(td.view(torch.int32), ref_d.view(torch.int32)))
+    del ref_ids, ref_d
+    st = sts[-1]
     ms_per_step = t_ms / args.steps
     value = n * world * args.steps / (t_ms / 1e3)
+    plain_steps = len(st_plain)
+    plain_value = n * world * plain_steps / (t_plain / 1e3)
 
     # ---- end to end through the host API, pinned buffers ------------------
     hx = torch.from_numpy(x).pin_memory()
     hids = torch.empty((n, K), dtype=torch.int32).pin_memory()
     hd = torch.empty((n, K), dtype=torch.float32).pin_memory()
     xs_np, ids_np, d_np = hx.numpy(), hids.numpy(), hd.numpy()
-    kj.selfjoin(xs_np, k, num_indexed_dims=di, beta=beta, out_ids=ids_np, out_dists=d_np)
+
+    def host_step():
+        kj.selfjoin(xs_np, k, num_indexed_dims=di, beta=beta, radius_mode=kj.RADIUS_LEARNED, out_ids=ids_np,
+                    out_dists=d_np)
+
+    host_step()
     torch.cuda.synchronize()
     dist.barrier()
     e2 = torch.cuda.Event(enable_timing=True)
@@ -258,7 +270,7 @@ def run_gb300(args):
     e2.record()
     e2e_steps = max(1, min(args.steps, 3))
     for _ in range(e2e_steps):
-        kj.selfjoin(xs_np, k, num_indexed_dims=di, beta=beta, out_ids=ids_np, out_dists=d_np)
+        host_step()
     e3.record()
     torch.cuda.synchronize()
     t_e2e = dist.max(e2.elapsed_time(e3))
@@ -266,30 +278,43 @@ def run_gb300(args):
 
     # ---- roofline of the dominant kernel (the search) ----------------------
     pk = peaks()
-    kms = statistics.median(kernel_ms)
-    ab = statistics.median(alg_bytes)
+    kms = statistics.median([s_["ms_search_kernels"] for s_ in sts])
+    ab = statistics.median([s_["search_alg_bytes"] for s_ in sts])
+    fl = statistics.median([s_["search_alg_flops"] for s_ in sts])
     achieved = ab / (kms / 1e3) / 1e9
     tr = ncu_traffic(WORKLOAD)
+    # second roof: the FP32 pipe (152 SMs x 128 lanes x 2 flops x clock)
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_ach = fl / (kms / 1e3) / 1e12
     roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"], "traffic": tr["dram_bytes_per_join"] if tr else None,
-                "kernel": "search_kernel<float,2>", "kernel_ms_per_step": kms,
-                "alg_bytes_per_step": ab, "peak_source": pk["source"] + " hbm_gbs (MEASURED_PEAKS.json)"}
+                "kernel": "search_kernel<float,2,2>", "kernel_ms_per_step": kms, "launches_per_step":
+                st["iterations"], "alg_bytes_per_step": ab,
+                "peak_source": f"{pk['source']} hbm_gbs (MEASURED_PEAKS.json): frac is of {pk['source']}",
+                "fp32": {"achieved_tflops": fp32_ach, "peak_tflops": fp32_peak, "frac": fp32_ach / fp32_peak,
+                         "alg_flops_per_step": fl, "peak_source": "nominal 152x128x2 x median SM clock"}}
+    launches = sum(int(s_["kernel_launches"]) for s_ in sts)
 
     line = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "n_points": n, "d": d, "k": k, "beta": beta, "num_indexed_dims": di,
-                   "radius": "plain BETA schedule", "parallelism": f"replicas x{world}",
+                   "radius": "learned starting radius (built-in model)", "parallelism": f"replicas x{world}",
                    "l2": "inputs (200 MB) and outputs (13 GB) exceed the 129 MB L2; no flush"},
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(n * d * 4),
                 "d2h_bytes_per_step": int(n * K * 8)},
-        "gpu_launches": int(launches),
+        "gpu_launches": launches,
         "roofline": roofline,
         "clocks": clk,
-        "search_iterations": statistics.median(iters),
-        "stats_last_step": {kk: st[kk] for kk in ("eps0", "iterations", "regrids", "candidates", "ms_prep",
-                                                  "ms_search", "ms_search_kernels", "nonempty_cells")},
+        "plain_beta": {"value": plain_value, "ms_per_step": t_plain / plain_steps, "steps": plain_steps,
+                       "iterations": st_plain[-1]["iterations"], "candidates": st_plain[-1]["candidates"],
+                       "ms_search_kernels": st_plain[-1]["ms_search_kernels"]},
+        "learned_over_plain": value / plain_value,
+        "identical_to_plain": identical,
+        "stats_last_step": {kk: st[kk] for kk in ("eps0", "iterations", "regrids", "candidates", "queries_run",
+                                                  "ms_prep", "ms_search", "ms_search_kernels", "nonempty_cells")},
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, k, beta, di, args.cpu_sample)
@@ -299,10 +324,11 @@ def run_gb300(args):
     return 0
 
 
-def run_profile_case(which: str):
+def run_profile_case(which: str, mode: str):
     """One device-resident join for profiler captures.  'full' is the bench
     workload; 'slice' is its longitude slice x < 57.6 deg (about 4M points,
-    the same densities), small enough for multi-pass ncu captures."""
+    the same densities), small enough for multi-pass ncu captures.  mode:
+    'learned' (the bench headline) or 'plain'."""
     import numpy as np
     import torch
 
@@ -315,9 +341,10 @@ def run_profile_case(which: str):
     tids = torch.empty((n, k + 1), dtype=torch.int32, device="cuda")
     td = torch.empty((n, k + 1), dtype=torch.float32, device="cuda")
     st = kj.selfjoin_device(tx.data_ptr(), np.float32, n, d, k, tids.data_ptr(), td.data_ptr(),
-                            num_indexed_dims=di, beta=beta)
+                            num_indexed_dims=di, beta=beta,
+                            radius_mode=kj.RADIUS_LEARNED if mode == "learned" else kj.RADIUS_PLAIN)
     torch.cuda.synchronize()
-    print(json.dumps({"case": which, "n": n, **{kk: st[kk] for kk in (
+    print(json.dumps({"case": which, "mode": mode, "n": n, **{kk: st[kk] for kk in (
         "eps0", "iterations", "regrids", "candidates", "queries_run", "ms_prep", "ms_search", "ms_search_kernels",
         "search_alg_bytes", "kernel_launches")}}), flush=True)
     return 0
@@ -333,6 +360,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-case", choices=["full", "slice"], default=None,
                     help="run one join for a profiler capture and exit")
+    ap.add_argument("--profile-mode", choices=["learned", "plain"], default="learned")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warning: fewer than 3 warm-up steps")
@@ -341,7 +369,7 @@ def main():
     import __graft_entry__
     __graft_entry__.build_library()
     if args.profile_case:
-        return run_profile_case(args.profile_case)
+        return run_profile_case(args.profile_case, args.profile_mode)
     return run_gb300(args)
 
 

@@ -83,12 +83,11 @@ __global__ void eps_avg_sample_kernel(const double* __restrict__ partial, uint64
   sample_sum[g] = s;
 }
 
-// One warp: the per-sample sums added in sample order.
-__global__ void eps_avg_final_kernel(const double* __restrict__ sample_sum, uint64_t n, uint64_t nthr,
+// One warp: the per-sample sums added in sample order; cnt = number of terms.
+__global__ void eps_avg_final_kernel(const double* __restrict__ sample_sum, uint64_t nthr, unsigned long long cnt,
                                      double* __restrict__ out) {
   const int lane = threadIdx.x & 31;
   double tot = 0.0;
-  unsigned long long cnt = 0;
   for (uint64_t b = 0; b < nthr; b += 32) {
     const uint64_t g = b + lane;
     const double v = g < nthr ? sample_sum[g] : 0.0;
@@ -98,8 +97,6 @@ __global__ void eps_avg_final_kernel(const double* __restrict__ sample_sum, uint
       if (b + j < nthr) tot = __dadd_rn(tot, x);
     }
   }
-  for (uint64_t g = 0; g < nthr; g++)
-    if (g * 1000 < n) cnt += terms_of_sample(g, n);
   if (lane == 0) {
     out[0] = __ddiv_rn(tot, (double)cnt);  // GPU.cu:3339: total/(cnt*1.0)
     out[1] = (double)cnt;
@@ -198,7 +195,12 @@ void launch_eps_avg(const T* soa, uint64_t n, uint32_t d, const EpsScratch& sc, 
     eps_avg_sample_kernel<<<(unsigned)((nthr + 255) / 256), 256, 0, s>>>(sc.partial, nthr, nch, sc.sample_sum);
     KNNSJ_CHECK_LAUNCH();
   }
-  eps_avg_final_kernel<<<1, 32, 0, s>>>(sc.sample_sum, n, nthr, sc.avg_out);
+  // number of distances summed (the reference counts them with an atomic,
+  // kernel.cu:366): every sample thread g with 1000*g < N
+  unsigned long long cnt = 0;
+  for (uint64_t g = 0; g < nthr; g++)
+    if (g * 1000 < n) cnt += terms_of_sample(g, n);
+  eps_avg_final_kernel<<<1, 32, 0, s>>>(sc.sample_sum, nthr, cnt, sc.avg_out);
   KNNSJ_CHECK_LAUNCH();
 }
 

@@ -43,8 +43,13 @@ namespace {
 
 constexpr int SEARCH_THREADS = 256;
 constexpr int QCHUNK = 4;
-#ifndef KNNSJ_WAVE_ROWS
-#define KNNSJ_WAVE_ROWS 4
+// ring rows per wave (each gives at most two runs of points): for one or two
+// indexed dimensions, and for more (wider rings of shorter rows)
+#ifndef KNNSJ_WAVE_ROWS_LO
+#define KNNSJ_WAVE_ROWS_LO 16
+#endif
+#ifndef KNNSJ_WAVE_ROWS_HI
+#define KNNSJ_WAVE_ROWS_HI 32
 #endif
 #ifndef KNNSJ_EARLY_FAIL
 #define KNNSJ_EARLY_FAIL 1
@@ -52,8 +57,29 @@ constexpr int QCHUNK = 4;
 #ifndef KNNSJ_SORT_ROWS
 #define KNNSJ_SORT_ROWS 1
 #endif
-constexpr int WAVE_ROWS = KNNSJ_WAVE_ROWS;  // rows per wave (each gives at most 2 runs)
-constexpr int MAX_RUNS = 2 * WAVE_ROWS;
+// rings of at most this many rows are scanned in their natural order (one or
+// two waves: sorting them by lower bound saves nothing)
+#ifndef KNNSJ_SORT_MIN_ROWS
+#define KNNSJ_SORT_MIN_ROWS 4
+#endif
+// intermediate threshold tightening once K keys are held: 0 only when the
+// buffer fills, 1 after every wave, 2 after every wave for a uniform radius
+// only (a per-query starting radius is already close to the K-th distance)
+// reduce before the output sort when more than 2K keys are held (the counting
+// sort handles up to 256 keys by itself)
+#ifndef KNNSJ_PRE_WRITE_REDUCE
+#define KNNSJ_PRE_WRITE_REDUCE 0
+#endif
+#ifndef KNNSJ_TIGHTEN
+#define KNNSJ_TIGHTEN 2
+#endif
+constexpr int MAX_WAVE_ROWS = KNNSJ_WAVE_ROWS_LO > KNNSJ_WAVE_ROWS_HI ? KNNSJ_WAVE_ROWS_LO : KNNSJ_WAVE_ROWS_HI;
+constexpr int MAX_RUNS = 2 * MAX_WAVE_ROWS;
+static_assert(MAX_WAVE_ROWS <= 32, "a wave is at most one row per lane");
+template <int DI>
+constexpr int wave_rows() {
+  return (DI > 0 && DI <= 2) ? KNNSJ_WAVE_ROWS_LO : KNNSJ_WAVE_ROWS_HI;
+}
 constexpr uint32_t HIST_MAX_B = 256;  // histogram reduce for buffers up to this size
 constexpr int WARP_WORDS = 256 + 2 * MAX_RUNS + 8;  // per-warp u32 scratch: bins, runS, runP
 
@@ -260,7 +286,7 @@ __device__ __noinline__ void write_sorted_row(typename Key<T>::type* buf, uint32
     const uint32_t i = r * 32 + lane;
     v[r] = Kt::maxv();
     slot[r] = 0;
-    if (i < len) {
+    if (r * 32 < (int)len && i < len) {
       v[r] = buf[i];
       const int b = min((int)((float)Kt::acc(v[r]) * scale), 255);
       slot[r] = atomicAdd(&cnt[b], 1u);
@@ -294,7 +320,7 @@ __device__ __noinline__ void write_sorted_row(typename Key<T>::type* buf, uint32
   for (int r = 0; r < R; r++) {
     const uint32_t i = r * 32 + lane;
     pos[r] = 0xffffffffu;
-    if (i < len) {
+    if (r * 32 < (int)len && i < len) {
       const int b = min((int)((float)Kt::acc(v[r]) * scale), 255);
       pos[r] = cnt[b] + slot[r];
       buf[pos[r]] = v[r];
@@ -305,12 +331,13 @@ __device__ __noinline__ void write_sorted_row(typename Key<T>::type* buf, uint32
 #pragma unroll
   for (int r = 0; r < R; r++) {
     const uint32_t i = r * 32 + lane;
-    if (i < len) {
+    if (r * 32 < (int)len && i < len) {
       const int b = min((int)((float)Kt::acc(v[r]) * scale), 255);
       const uint32_t first = cnt[b];
       const uint32_t last = b < 255 ? cnt[b + 1] : len;
       uint32_t rank = 0;
-      for (uint32_t j = first; j < last; j++) rank += Kt::less(buf[j], v[r]) ? 1u : 0u;
+      if (first < K)
+        for (uint32_t j = first; j < last; j++) rank += Kt::less(buf[j], v[r]) ? 1u : 0u;
       const uint32_t fin = first + rank;
       if (fin < K) {
         out_ids[row_out + fin] = (int32_t)Kt::id(v[r]);
@@ -357,13 +384,23 @@ __device__ __forceinline__ unsigned long long warp_sort32(unsigned long long v, 
   return v;
 }
 
-#ifndef KNNSJ_SEARCH_MIN_BLOCKS
-#define KNNSJ_SEARCH_MIN_BLOCKS 3
+// resident blocks per SM the register budget is cut for: low dimensions
+// (d <= 3) fit 64 registers without spilling, higher ones need more
+#ifndef KNNSJ_MINB_LO
+#define KNNSJ_MINB_LO 4
 #endif
+#ifndef KNNSJ_MINB_HI
+#define KNNSJ_MINB_HI 3
+#endif
+template <int D>
+constexpr int search_min_blocks() {
+  return (D > 0 && D <= 3) ? KNNSJ_MINB_LO : KNNSJ_MINB_HI;
+}
 
 // D: data dimensions (0 = runtime); DI: indexed dimensions (0 = runtime, <= MAX_DI).
 template <typename T, int D, int DI>
-__global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) search_kernel(const SearchParams<T> p) {
+__global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search_kernel(const SearchParams<T> p) {
+  constexpr int WAVE_ROWS = wave_rows<DI>();
   constexpr int NDI = DI > 0 ? DI : MAX_DI;
   using Kt = Key<T>;
   using KT = typename Kt::type;
@@ -504,6 +541,8 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
       // rows of the ring in groups of 32 sorted by lower bound, a wave of
       // WAVE_ROWS rows at a time.  One scan loop consumes them all.
       bool own_pending = !fail_now;
+      const bool sorted_rows = KNNSJ_SORT_ROWS && nrows > KNNSJ_SORT_MIN_ROWS;
+      const bool tighten = KNNSJ_TIGHTEN == 1 || (KNNSJ_TIGHTEN == 2 && p.qradius == nullptr);
       unsigned long long g0 = 0;   // first row of the current group
       int nvalid = 0, w0 = 0;      // rows in the group, next wave start
       unsigned long long skey = 0, rbase = 0;
@@ -535,7 +574,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
             rcenter = false;
             if (ridx < nrows) rlb = row_info((uint32_t)ridx, rbase, rcenter);
             skey = ((unsigned long long)__float_as_uint(rlb) << 32) | (unsigned long long)(uint32_t)lane;
-            if (KNNSJ_SORT_ROWS) skey = warp_sort32(skey, lane);
+            if (sorted_rows) skey = warp_sort32(skey, lane);
             nvalid = (int)min(32ull, nrows - g0);
             w0 = 0;
           }
@@ -549,7 +588,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
           const bool have = st.len >= K;
           // rows come in ascending lower bound: the rest of the group can go
           const float first_lb = __shfl_sync(FULL, lbs, 0);
-          if (KNNSJ_SORT_ROWS && have && first_lb > tup) {
+          if (sorted_rows && have && first_lb > tup) {
             w0 = nvalid;
             continue;
           }
@@ -597,7 +636,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
             runP[2 * lane] = ex;
             runP[2 * lane + 1] = ex + la;
           }
-          nr = MAX_RUNS;
+          nr = 2 * WAVE_ROWS;
           w0 += WAVE_ROWS;
         }
         __syncwarp();
@@ -637,14 +676,16 @@ __global__ void __launch_bounds__(SEARCH_THREADS, KNNSJ_SEARCH_MIN_BLOCKS) searc
         }
         scanned += total;
         __syncwarp();
-        if (!st.tight && st.len >= K) st = reduce<T>(buf, hist, st, K, B, lane);
+        if (tighten && !st.tight && st.len >= K) st = reduce<T>(buf, hist, st, K, B, lane);
       }
 
       __syncwarp();
       if (st.len >= K) {
         const uint64_t row_out = (uint64_t)qid * K;
         if (B <= HIST_MAX_B) {
+#if KNNSJ_PRE_WRITE_REDUCE
           if (st.len > 2 * K && st.len > 64) st = reduce<T>(buf, hist, st, K, B, lane);
+#endif
           write_sorted_row<T>(buf, hist, st.len, st.tau, K, p.out_ids, p.out_d, row_out, lane);
         } else {
           write_sorted_row_bitonic<T>(buf, st.len, K, p.out_ids, p.out_d, row_out, lane);
