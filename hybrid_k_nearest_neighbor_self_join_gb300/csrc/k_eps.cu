@@ -7,7 +7,8 @@
 //     one double with atomicAdd, so its mean varies in the last bits from run
 //     to run.  Here the order is fixed: sample g's distances are summed in
 //     chunks of EPS_CHUNK consecutive terms, the chunk sums in chunk order,
-//     then the per-sample sums in sample order -- the order the oracle uses.
+//     then the per-sample sums in 32 contiguous groups of samples (each in
+//     sample order, the group sums in group order) -- the oracle's order.
 //   * kernelKDistBruteForce (kernel.cu:450-523): block b takes point
 //     b*offset and bins its distances below the mean to every 8th block of
 //     256 points into 10 000 buckets of width mean/10000, 8 counts per hit.
@@ -64,11 +65,22 @@ __global__ void eps_avg_chunk_kernel(const T* __restrict__ soa, uint64_t n, uint
   if (tid < n) {
     const uint64_t t = g % EPS_BLOCK;
     const uint64_t m_end = min(terms_of_sample(g, n), (uint64_t)(c + 1) * EPS_CHUNK);
-    for (uint64_t m = (uint64_t)c * EPS_CHUNK; m < m_end; m++) {
-      const uint64_t i = t + 1000 * m;
-      double rd = 0.0;
-      for (uint32_t l = 0; l < d; l++) rd = eps_term(rd, soa[(uint64_t)l * n + i], soa[(uint64_t)l * n + tid]);
-      s = __dadd_rn(s, __dsqrt_rn(rd));
+    // four terms at a time: their loads are independent; the sum still runs
+    // term by term in ascending order
+    constexpr int U = 4;
+    for (uint64_t m = (uint64_t)c * EPS_CHUNK; m < m_end; m += U) {
+      double rd[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) rd[u] = 0.0;
+      for (uint32_t l = 0; l < d; l++) {
+        const T ql = soa[(uint64_t)l * n + tid];
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          if (m + u < m_end) rd[u] = eps_term(rd[u], soa[(uint64_t)l * n + t + 1000 * (m + u)], ql);
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (m + u < m_end) s = __dadd_rn(s, __dsqrt_rn(rd[u]));
     }
   }
   partial[w] = s;
@@ -83,20 +95,18 @@ __global__ void eps_avg_sample_kernel(const double* __restrict__ partial, uint64
   sample_sum[g] = s;
 }
 
-// One warp: the per-sample sums added in sample order; cnt = number of terms.
+// One warp: lane j adds the per-sample sums of the j-th of 32 contiguous
+// groups of samples in sample order, then the 32 group sums are added in
+// group order; cnt = number of terms.
 __global__ void eps_avg_final_kernel(const double* __restrict__ sample_sum, uint64_t nthr, unsigned long long cnt,
                                      double* __restrict__ out) {
   const int lane = threadIdx.x & 31;
+  const uint64_t group = (nthr + 31) / 32;
+  const uint64_t g_end = min(nthr, (uint64_t)(lane + 1) * group);
+  double gs = 0.0;
+  for (uint64_t g = (uint64_t)lane * group; g < g_end; g++) gs = __dadd_rn(gs, sample_sum[g]);
   double tot = 0.0;
-  for (uint64_t b = 0; b < nthr; b += 32) {
-    const uint64_t g = b + lane;
-    const double v = g < nthr ? sample_sum[g] : 0.0;
-#pragma unroll 8
-    for (int j = 0; j < 32; j++) {
-      const double x = __shfl_sync(FULL, v, j);
-      if (b + j < nthr) tot = __dadd_rn(tot, x);
-    }
-  }
+  for (int j = 0; j < 32; j++) tot = __dadd_rn(tot, __shfl_sync(FULL, gs, j));
   if (lane == 0) {
     out[0] = __ddiv_rn(tot, (double)cnt);  // GPU.cu:3339: total/(cnt*1.0)
     out[1] = (double)cnt;
@@ -131,29 +141,49 @@ __global__ void __launch_bounds__(EPS_BLOCK) eps_hist_kernel(const T* __restrict
   const float errc = (float)(2 * d + 8) * 5.9604645e-8f;  // (2d+8) * 2^-24, relative
   const float abs_q = (float)(abs_err / bw) * 1.0001f + 1e-4f;
   const float flo = (float)b_lo, fhi = (float)b_hi;
-  for (uint64_t i = 0; i < n; i += (uint64_t)EPS_BLOCK * 8) {
-    const uint64_t p = i + threadIdx.x;
-    if (p >= n || p == sid) continue;
-    float s32 = 0.0f;
+  // the sample point's coordinates once per block; four candidates per
+  // thread and round so that their loads overlap
+  __shared__ T qs[MAX_D];
+  for (uint32_t l = threadIdx.x; l < d; l += blockDim.x) qs[l] = soa[(uint64_t)l * n + sid];
+  __syncthreads();
+  constexpr uint64_t STEP = (uint64_t)EPS_BLOCK * 8;
+  constexpr int U = 4;
+  for (uint64_t i0 = 0; i0 < n; i0 += STEP * U) {
+    float s4[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) s4[u] = 0.0f;
     for (uint32_t l = 0; l < d; l++) {
-      const float df = __fsub_rn((float)soa[(uint64_t)l * n + p], (float)soa[(uint64_t)l * n + sid]);
-      s32 = __fadd_rn(s32, __fmul_rn(df, df));
+      const float qf = (float)qs[l];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const uint64_t p = i0 + u * STEP + threadIdx.x;
+        if (p < n) {
+          const float df = __fsub_rn((float)soa[(uint64_t)l * n + p], qf);
+          s4[u] = __fadd_rn(s4[u], __fmul_rn(df, df));
+        }
+      }
     }
-    const float q32 = __fmul_rn(__fsqrt_rn(s32), inv_bw);
-    const float del = __fmaf_rn(errc, q32, abs_q);
-    if (q32 - del >= 10000.5f) continue;  // certainly not below the mean
-    if (q32 + del < flo) continue;        // below this bucket range
-    if (q32 - del >= fhi) continue;       // above this bucket range
-    uint32_t bucket;
-    const float fb = floorf(q32);
-    if (q32 + del < 9999.9f && q32 - del > fb && q32 + del < fb + 1.0f) {
-      bucket = (uint32_t)fb;
-    } else {
-      double rd = 0.0;
-      for (uint32_t l = 0; l < d; l++) rd = eps_term(rd, soa[(uint64_t)l * n + p], soa[(uint64_t)l * n + sid]);
-      bucket = exact_bucket(rd, avg, bw);
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const uint64_t p = i0 + u * STEP + threadIdx.x;
+      if (p >= n || p == sid) continue;
+      const float s32 = s4[u];
+      const float q32 = __fmul_rn(__fsqrt_rn(s32), inv_bw);
+      const float del = __fmaf_rn(errc, q32, abs_q);
+      if (q32 - del >= 10000.5f) continue;  // certainly not below the mean
+      if (q32 + del < flo) continue;        // below this bucket range
+      if (q32 - del >= fhi) continue;       // above this bucket range
+      uint32_t bucket;
+      const float fb = floorf(q32);
+      if (q32 + del < 9999.9f && q32 - del > fb && q32 + del < fb + 1.0f) {
+        bucket = (uint32_t)fb;
+      } else {
+        double rd = 0.0;
+        for (uint32_t l = 0; l < d; l++) rd = eps_term(rd, soa[(uint64_t)l * n + p], qs[l]);
+        bucket = exact_bucket(rd, avg, bw);
+      }
+      if (bucket >= b_lo && bucket < b_hi) atomicAdd(&sh[bucket - b_lo], 8u);
     }
-    if (bucket >= b_lo && bucket < b_hi) atomicAdd(&sh[bucket - b_lo], 8u);
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x)

@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(RA_THREADS) radius_assign_kernel(const CellTab
                                                                    const float* __restrict__ model, float eps0f,
                                                                    float log_lo, float log_hi, float offset,
                                                                    T* __restrict__ qradius) {
-  __shared__ float sm[MODEL_FLOATS];
+  __shared__ __align__(16) float sm[MODEL_FLOATS + 3];
   for (int i = threadIdx.x; i < MODEL_FLOATS; i += blockDim.x) sm[i] = model[i];
   __syncthreads();
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(RA_THREADS) radius_assign_kernel(const CellTab
   for (uint32_t j = 0; j < t.g.di; j++) q[j] = ps[(uint64_t)j * n + i];
   float f[NFEAT];
   radius_features(t, q, d, k, beta, n, f);
-  float y = mlp_eval(sm, f) + offset;
+  float y = mlp_eval_blocked(sm, f) + offset;
   y = fminf(fmaxf(y, log_lo), log_hi);
   qradius[pid[i]] = (T)(eps0f * expf(y));
 }
@@ -96,14 +96,14 @@ __global__ void __launch_bounds__(RA_THREADS) radius_features_kernel(const CellT
 __global__ void __launch_bounds__(RA_THREADS) mlp_predict_kernel(const float* __restrict__ model,
                                                                  const float* __restrict__ feat, uint64_t n,
                                                                  float* __restrict__ out) {
-  __shared__ float sm[MODEL_FLOATS];
+  __shared__ __align__(16) float sm[MODEL_FLOATS + 3];
   for (int i = threadIdx.x; i < MODEL_FLOATS; i += blockDim.x) sm[i] = model[i];
   __syncthreads();
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float f[NFEAT];
   for (int j = 0; j < NFEAT; j++) f[j] = feat[i * NFEAT + j];
-  out[i] = mlp_eval(sm, f);
+  out[i] = mlp_eval_blocked(sm, f);
 }
 
 }  // namespace

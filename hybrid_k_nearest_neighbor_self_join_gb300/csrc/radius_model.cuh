@@ -144,29 +144,55 @@ __device__ void radius_features(const CellTable<T>& t, const T* q, uint32_t d, u
   (void)n;
 }
 
-// Model output for one feature vector (one thread).  model may live in
-// shared or global memory; all threads of a warp read the same weights.
-__device__ __forceinline__ float mlp_eval(const float* __restrict__ model, const float* f) {
+// Model output for one feature vector (one thread).  Every sum runs in a
+// fixed order: first layer h = b1 + sum_i x_i W1[i][h] (i ascending), second
+// layer a = b2 + sum_i relu(h_i) W2[i][o] (i ascending), y = b3 + sum_o
+// relu(a_o) W3[o] (o ascending), so the training kernels and a numpy
+// restatement reproduce it.  The loops are turned so that the weights are
+// read as vector rows: the 64 second-layer sums stay in registers while the
+// first layer is produced 16 hidden units at a time and consumed at once.
+// The model must be 16-byte aligned (shared memory in practice).
+__device__ __forceinline__ float mlp_eval_blocked(const float* __restrict__ model, const float* f) {
   float x[NFEAT];
 #pragma unroll
   for (int i = 0; i < NFEAT; i++) x[i] = (f[i] - model[M_MEAN + i]) * model[M_ISTD + i];
-  float h1[NHID];
+  float a[NHID];
 #pragma unroll
-  for (int h = 0; h < NHID; h++) h1[h] = model[M_B1 + h];
+  for (int o = 0; o < NHID; o++) a[o] = model[M_B2 + o];
+#pragma unroll 1
+  for (int hc = 0; hc < NHID; hc += 16) {
+    float h1[16];
 #pragma unroll
-  for (int i = 0; i < NFEAT; i++) {
+    for (int h = 0; h < 16; h++) h1[h] = model[M_B1 + hc + h];
 #pragma unroll
-    for (int h = 0; h < NHID; h++) h1[h] = fmaf(x[i], model[M_W1 + i * NHID + h], h1[h]);
+    for (int i = 0; i < NFEAT; i++) {
+      const float4* w = reinterpret_cast<const float4*>(model + M_W1 + i * NHID + hc);
+#pragma unroll
+      for (int h4 = 0; h4 < 4; h4++) {
+        const float4 wv = w[h4];
+        h1[4 * h4 + 0] = fmaf(x[i], wv.x, h1[4 * h4 + 0]);
+        h1[4 * h4 + 1] = fmaf(x[i], wv.y, h1[4 * h4 + 1]);
+        h1[4 * h4 + 2] = fmaf(x[i], wv.z, h1[4 * h4 + 2]);
+        h1[4 * h4 + 3] = fmaf(x[i], wv.w, h1[4 * h4 + 3]);
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < 16; h++) {
+      const float hv = fmaxf(h1[h], 0.0f);
+      const float4* w = reinterpret_cast<const float4*>(model + M_W2 + (hc + h) * NHID);
+#pragma unroll
+      for (int o4 = 0; o4 < NHID / 4; o4++) {
+        const float4 wv = w[o4];
+        a[4 * o4 + 0] = fmaf(hv, wv.x, a[4 * o4 + 0]);
+        a[4 * o4 + 1] = fmaf(hv, wv.y, a[4 * o4 + 1]);
+        a[4 * o4 + 2] = fmaf(hv, wv.z, a[4 * o4 + 2]);
+        a[4 * o4 + 3] = fmaf(hv, wv.w, a[4 * o4 + 3]);
+      }
+    }
   }
-#pragma unroll
-  for (int h = 0; h < NHID; h++) h1[h] = fmaxf(h1[h], 0.0f);
   float y = model[M_B3];
-  for (int o = 0; o < NHID; o++) {
-    float a = model[M_B2 + o];
 #pragma unroll
-    for (int i = 0; i < NHID; i++) a = fmaf(h1[i], model[M_W2 + i * NHID + o], a);
-    y = fmaf(fmaxf(a, 0.0f), model[M_W3 + o], y);
-  }
+  for (int o = 0; o < NHID; o++) y = fmaf(fmaxf(a[o], 0.0f), model[M_W3 + o], y);
   return y;
 }
 

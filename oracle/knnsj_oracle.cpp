@@ -117,7 +117,8 @@ inline double fma_t(double a, double b, double c) { return std::fma(a, b, c); }
 //
 // Deviations, all documented in the returned statistics' meaning:
 //   * the mean distance is summed per sample thread in chunks of 256 terms
-//     (chunk sums added in order), then over sample threads in thread order
+//     (chunk sums added in order), then over sample threads: 32 contiguous
+//     groups of threads each in thread order, the group sums in group order
 //     (the reference uses a double atomicAdd, whose order -- and so the last
 //     bits of the mean -- varies run to run);
 //   * histogram reads past N (kernel.cu:486-492 leaves i+threadIdx.x
@@ -171,12 +172,17 @@ EpsResult estimate_epsilon(const T* X, uint64_t n, uint32_t d, uint32_t k,
     partial[g] = s;
     pcount[g] = c;
   }
+  // per-thread sums: 32 contiguous groups of threads, each summed in thread
+  // order, then the 32 group sums in group order (the CUDA path's order)
   double total = 0.0;
   uint64_t cnt = 0;
-  for (uint64_t g = 0; g < nthr; g++) {
-    total += partial[g];
-    cnt += pcount[g];
+  const uint64_t group = (nthr + 31) / 32;
+  for (uint64_t j = 0; j < 32; j++) {
+    double gs = 0.0;
+    for (uint64_t g = j * group; g < std::min(nthr, (j + 1) * group); g++) gs += partial[g];
+    total += gs;
   }
+  for (uint64_t g = 0; g < nthr; g++) cnt += pcount[g];
   r.pair_count = cnt;
   r.avg = total / (cnt * 1.0);  // GPU.cu:3339
 
