@@ -4,12 +4,16 @@
 // (join.cu).
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstddef>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #ifdef KNNSJ_BUILD_DTYPE_DOUBLE
@@ -135,9 +139,8 @@ void init_stats(knnsj_stats* st) {
 }
 
 template <typename T>
-void host_join(const T* data, uint64_t n, uint32_t d, uint32_t k, const JoinConfig& cfg, int dev,
-               int32_t* out_ids, T* out_d, knnsj_stats* st) {
-  Workspace& w = ready_workspace(dev);
+void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t k, const JoinConfig& cfg,
+                  int32_t* out_ids, T* out_d, knnsj_stats* st, bool checksum) {
   cudaStream_t s = w.stream;
   const uint64_t K = (uint64_t)k + 1;
   T* din = (T*)w.in.get(n * d * sizeof(T));
@@ -150,7 +153,7 @@ void host_join(const T* data, uint64_t n, uint32_t d, uint32_t k, const JoinConf
   KNNSJ_CUDA(cudaMemcpyAsync(din, data, n * d * sizeof(T), cudaMemcpyHostToDevice, s));
   KNNSJ_CUDA(cudaEventRecord(t1, s));
   run_join<T>(w, cfg, din, data, n, d, k, dids, ddist, st, s);
-  if (st) st->total_distance = device_checksum<T>(w, ddist, n * K, s);
+  if (st && checksum) st->total_distance = device_checksum<T>(w, ddist, n * K, s);
   cudaEvent_t t2, t3;
   KNNSJ_CUDA(cudaEventCreate(&t2));
   KNNSJ_CUDA(cudaEventCreate(&t3));
@@ -178,11 +181,170 @@ void host_join(const T* data, uint64_t n, uint32_t d, uint32_t k, const JoinConf
 }
 
 template <typename T>
+void host_join(const T* data, uint64_t n, uint32_t d, uint32_t k, const JoinConfig& cfg, int dev,
+               int32_t* out_ids, T* out_d, knnsj_stats* st) {
+  host_join_ws<T>(ready_workspace(dev), data, n, d, k, cfg, out_ids, out_d, st, true);
+}
+
+template <typename T>
 void device_join(const T* data, uint64_t n, uint32_t d, uint32_t k, const JoinConfig& cfg, int dev,
                  int32_t* out_ids, T* out_d, knnsj_stats* st) {
   Workspace& w = ready_workspace(dev);
   run_join<T>(w, cfg, data, nullptr, n, d, k, out_ids, out_d, st, w.stream);
   KNNSJ_CUDA(cudaStreamSynchronize(w.stream));
+}
+
+// ---- batched self-joins (knnsj_selfjoin_batched) ---------------------------
+// Many independent joins of uneven sizes.  One small set keeps the GPU busy
+// for a fraction of the time its launches and host synchronisations take, so
+// worker host threads, each with its own workspace and stream, take the sets
+// largest first and run them side by side.  The search kernel's launch shape
+// (warps per block, queries per work fetch, selection buffer) is chosen per
+// (dtype, d, indexed dims, K) class by an autotuner: the first time a class
+// appears in the process, every candidate shape runs the class's largest set
+// and the fastest search is kept.  Shapes change only speed: every set's
+// result equals that of a knnsj_selfjoin call on it.
+
+struct ShapeKey {
+  int dtype;
+  uint32_t d, di, K;
+  bool operator<(const ShapeKey& o) const {
+    if (dtype != o.dtype) return dtype < o.dtype;
+    if (d != o.d) return d < o.d;
+    if (di != o.di) return di < o.di;
+    return K < o.K;
+  }
+};
+
+std::map<ShapeKey, SearchShape> g_tuned;  // guarded by g_call_mutex
+
+std::vector<SearchShape> candidate_shapes(uint32_t K) {
+  std::vector<SearchShape> v;
+  for (int wpb : {4, 8})
+    for (int qc : {1, 4, 16}) {
+      SearchShape sh;
+      sh.warps_per_block = wpb;
+      sh.qchunk = qc;
+      v.push_back(sh);
+    }
+  if (K + 32 <= 256) {  // the sorted-buffer selection instead of the histogram one
+    SearchShape sh;
+    sh.warps_per_block = 8;
+    sh.qchunk = 4;
+    sh.buffer = 512;
+    v.push_back(sh);
+  }
+  return v;
+}
+
+struct BatchPool {
+  std::vector<Workspace*> ws;  // one per worker, kept across calls
+};
+
+BatchPool& batch_pool(int dev) {
+  static std::vector<BatchPool*> all;
+  if ((int)all.size() <= dev) all.resize(dev + 1, nullptr);
+  if (!all[dev]) all[dev] = new BatchPool();
+  return *all[dev];
+}
+
+int batch_workers(uint32_t n_sets) {
+  int w = 8;
+  if (const char* e = env("KNNSJ_BATCH_WORKERS")) w = std::max(1, std::atoi(e));
+  return (int)std::min<uint32_t>((uint32_t)w, std::max<uint32_t>(n_sets, 1));
+}
+
+template <typename T>
+void run_batched(knnsj_set* sets, const std::vector<uint32_t>& order, const std::vector<JoinConfig>& cfgs,
+                 int dev, knnsj_stats* agg) {
+  BatchPool& pool = batch_pool(dev);
+  const int nw = batch_workers((uint32_t)order.size());
+  while ((int)pool.ws.size() < nw) pool.ws.push_back(new Workspace());
+  for (int i = 0; i < nw; i++) {
+    pool.ws[i]->ensure_stream();
+    if (!pool.ws[i]->sm_count)
+      KNNSJ_CUDA(cudaDeviceGetAttribute(&pool.ws[i]->sm_count, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const int code = sizeof(T) == 4 ? KNNSJ_F32 : KNNSJ_F64;
+  auto key_of = [&](uint32_t i) {
+    return ShapeKey{code, sets[i].d, cfgs[i].num_indexed_dims, sets[i].k + 1};
+  };
+  auto join_one = [&](Workspace& w, uint32_t i, const SearchShape& sh, knnsj_stats* st) {
+    JoinConfig c = cfgs[i];
+    c.search_warps = sh.warps_per_block;
+    c.search_qchunk = sh.qchunk;
+    c.search_buffer = sh.buffer;
+    host_join_ws<T>(w, (const T*)sets[i].data, sets[i].n, sets[i].d, sets[i].k, c, sets[i].out_ids,
+                    (T*)sets[i].out_dists, st, false);
+  };
+  // autotune the classes seen for the first time, on their largest set
+  const char* at = env("KNNSJ_AUTOTUNE");
+  const bool tune = !(at && std::atoi(at) == 0);
+  std::map<ShapeKey, uint32_t> largest;
+  for (uint32_t i : order) {
+    if (sets[i].status != KNNSJ_OK) continue;
+    const ShapeKey kk = key_of(i);
+    if (!largest.count(kk) || sets[i].n > sets[largest[kk]].n) largest[kk] = i;
+  }
+  for (const auto& kv : largest) {
+    if (g_tuned.count(kv.first)) continue;
+    SearchShape best;
+    if (tune && sets[kv.second].n >= 20000) {
+      Workspace& w = *pool.ws[0];
+      knnsj_stats st;
+      std::memset(&st, 0, sizeof(st));
+      st.struct_size = sizeof(st);
+      try {
+        join_one(w, kv.second, best, &st);  // warm-up with the default shape
+        double best_ms = st.ms_search_kernels;
+        for (const SearchShape& sh : candidate_shapes(kv.first.K)) {
+          join_one(w, kv.second, sh, &st);
+          if (st.ms_search_kernels < best_ms * 0.98) {
+            best_ms = st.ms_search_kernels;
+            best = sh;
+          }
+        }
+      } catch (...) {
+        best = SearchShape();  // the set itself reports its error below
+      }
+    }
+    g_tuned[kv.first] = best;
+  }
+  // run every set; workers take them largest first
+  std::atomic<uint32_t> next{0};
+  std::vector<knnsj_stats> per(order.size());
+  auto worker = [&](int wi) {
+    cudaSetDevice(dev);
+    Workspace& w = *pool.ws[wi];
+    for (;;) {
+      const uint32_t slot = next.fetch_add(1);
+      if (slot >= order.size()) break;
+      const uint32_t i = order[slot];
+      if (sets[i].status != KNNSJ_OK) continue;
+      knnsj_stats& st = per[slot];
+      std::memset(&st, 0, sizeof(st));
+      st.struct_size = sizeof(st);
+      const SearchShape sh = g_tuned.find(key_of(i))->second;  // every valid set's class is tuned above
+      sets[i].status = guarded([&] { join_one(w, i, sh, &st); }, nullptr);
+    }
+  };
+  std::vector<std::thread> th;
+  for (int wi = 1; wi < nw; wi++) th.emplace_back(worker, wi);
+  worker(0);
+  for (auto& t : th) t.join();
+  for (const knnsj_stats& st : per) {
+    agg->iterations += st.iterations;
+    agg->regrids += st.regrids;
+    agg->candidates += st.candidates;
+    agg->queries_run += st.queries_run;
+    agg->ms_prep += st.ms_prep;
+    agg->ms_search += st.ms_search;
+    agg->ms_transfer += st.ms_transfer;
+    agg->ms_search_kernels += st.ms_search_kernels;
+    agg->search_alg_bytes += st.search_alg_bytes;
+    agg->search_alg_flops += st.search_alg_flops;
+    agg->kernel_launches += st.kernel_launches;
+  }
 }
 
 // ---- fixed-scratch join (knnsj_selfjoin_device_noalloc) --------------------
@@ -342,29 +504,39 @@ knnsj_status knnsj_selfjoin_device_noalloc(const void* d_data, knnsj_dtype dtype
 knnsj_status knnsj_selfjoin_batched(uint32_t n_sets, knnsj_set* sets, knnsj_dtype dtype,
                                     const knnsj_options* opts, knnsj_stats* stats) {
   if (n_sets > 0 && !sets) return KNNSJ_ERR_INVALID_ARGUMENT;
-  knnsj_status first = KNNSJ_OK;
+  if (dtype != KNNSJ_F32 && dtype != KNNSJ_F64) return KNNSJ_ERR_INVALID_ARGUMENT;
+  std::vector<JoinConfig> cfgs(n_sets);
+  std::vector<uint32_t> order;
+  for (uint32_t i = 0; i < n_sets; i++) {
+    knnsj_set& st = sets[i];
+    st.status = validate(st.data, st.n, st.d, st.k, st.out_ids, st.out_dists);
+    if (st.status == KNNSJ_OK) st.status = make_config(opts, st.d, &cfgs[i]);
+    order.push_back(i);
+  }
+  // largest first: the long sets start early and the short ones fill the gaps
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return sets[a].n > sets[b].n; });
+  std::lock_guard<std::mutex> lock(g_call_mutex);
   knnsj_stats agg;
   std::memset(&agg, 0, sizeof(agg));
-  for (uint32_t i = 0; i < n_sets; i++) {
-    knnsj_stats one;
-    std::memset(&one, 0, sizeof(one));
-    one.struct_size = sizeof(one);
-    sets[i].status = knnsj_selfjoin(sets[i].data, dtype, sets[i].n, sets[i].d, sets[i].k, opts,
-                                    sets[i].out_ids, sets[i].out_dists, &one);
-    if (sets[i].status != KNNSJ_OK && first == KNNSJ_OK) first = sets[i].status;
-    agg.iterations += one.iterations;
-    agg.candidates += one.candidates;
-    agg.queries_run += one.queries_run;
-    agg.ms_total += one.ms_total;
-    agg.ms_prep += one.ms_prep;
-    agg.ms_search += one.ms_search;
-    agg.ms_transfer += one.ms_transfer;
-  }
+  const auto t0 = std::chrono::steady_clock::now();
+  knnsj_status call = guarded(
+      [&] {
+        const int dev = select_device(opts);
+        if (dtype == KNNSJ_F32)
+          run_batched<float>(sets, order, cfgs, dev, &agg);
+        else
+          run_batched<double>(sets, order, cfgs, dev, &agg);
+      },
+      nullptr);
+  agg.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (stats) {
     agg.struct_size = stats->struct_size ? stats->struct_size : (uint32_t)sizeof(agg);
     *stats = agg;
   }
-  return first;
+  if (call != KNNSJ_OK) return call;
+  for (uint32_t i = 0; i < n_sets; i++)
+    if (sets[i].status != KNNSJ_OK) return sets[i].status;
+  return KNNSJ_OK;
 }
 
 knnsj_status knnsj_get_radius_model(float* out) {
@@ -498,6 +670,7 @@ void knnsj_release(void) {
     return;
   }
   workspace(dev).release_all();
+  for (Workspace* w : batch_pool(dev).ws) w->release_all();
 }
 
 // KNNJoinPy (main.cu:514): same symbol and arguments; returns nothing.

@@ -32,7 +32,7 @@
 
 namespace knnsj {
 
-unsigned long long g_launches = 0;
+thread_local unsigned long long g_launches = 0;
 
 void* Arena::take(size_t bytes) {
   const size_t at = (used + 255) & ~(size_t)255;
@@ -421,6 +421,9 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   a.work_counter = &sm->work_counter;
   a.rmax_bits = &sm->rmax_bits;
   a.qradius = qrad;
+  a.shape.warps_per_block = cfg.search_warps;
+  a.shape.qchunk = cfg.search_qchunk;
+  a.shape.buffer = cfg.search_buffer;
   T r = P.eps0;
   const double step = (double)P.eps0 * 0.5;
   a.step = (T)step;

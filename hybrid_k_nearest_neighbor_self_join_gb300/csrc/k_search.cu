@@ -41,8 +41,8 @@ namespace knnsj {
 
 namespace {
 
-constexpr int SEARCH_THREADS = 256;
-constexpr int QCHUNK = 4;
+constexpr int SEARCH_THREADS = 256;  // largest block; the launch may use fewer warps
+constexpr int QCHUNK = 4;            // default queries per work fetch
 // ring rows per wave (each gives at most two runs of points): for one or two
 // indexed dimensions, and for more (wider rings of shorter rows)
 #ifndef KNNSJ_WAVE_ROWS_LO
@@ -98,6 +98,7 @@ struct SearchParams {
   uint32_t d;
   uint32_t K;
   uint32_t B;
+  uint32_t qchunk;
   const uint32_t* __restrict__ qlist;
   uint32_t nq;
   T radius;
@@ -424,10 +425,10 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search
 
   for (;;) {
     uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(p.work_counter, (uint32_t)QCHUNK);
+    if (lane == 0) base = atomicAdd(p.work_counter, p.qchunk);
     base = __shfl_sync(FULL, base, 0);
     if (base >= p.nq) break;
-    const uint32_t qend = min(base + (uint32_t)QCHUNK, p.nq);
+    const uint32_t qend = min(base + p.qchunk, p.nq);
     for (uint32_t qi = base; qi < qend; ++qi) {
       // first pass: every point in cell order; later passes: the failed
       // queries by original id (valid across grid rebuilds)
@@ -707,11 +708,12 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search
 }
 
 template <typename T, int D, int DI>
-void launch_one(const SearchParams<T>& prm, int sm_count, cudaStream_t s) {
+void launch_one(const SearchParams<T>& prm, int wpb_req, int sm_count, cudaStream_t s) {
   // per-warp shared memory: selection buffer, u32 scratch, query copy (generic d)
   const size_t per_warp = (size_t)prm.B * sizeof(typename Key<T>::type) + WARP_WORDS * 4 +
                           (D == 0 ? (size_t)MAX_D * sizeof(T) : 0);
   int wpb = SEARCH_THREADS / 32;
+  if (wpb_req > 0 && wpb_req < wpb) wpb = wpb_req;
   while (wpb > 1 && per_warp * wpb > 200 * 1024) wpb--;
   const size_t smem = per_warp * wpb;
   auto kern = search_kernel<T, D, DI>;
@@ -719,7 +721,7 @@ void launch_one(const SearchParams<T>& prm, int sm_count, cudaStream_t s) {
   int per_sm = 0;
   KNNSJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, wpb * 32, smem));
   if (per_sm < 1) throw StatusError{KNNSJ_ERR_UNSUPPORTED, "search kernel does not fit"};
-  const uint64_t warps_needed = (prm.nq + QCHUNK - 1) / QCHUNK;
+  const uint64_t warps_needed = (prm.nq + prm.qchunk - 1) / prm.qchunk;
   uint64_t blocks = (uint64_t)per_sm * sm_count;
   const uint64_t need_blocks = (warps_needed + wpb - 1) / wpb;
   if (need_blocks < blocks) blocks = need_blocks;
@@ -755,6 +757,11 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s) {
   p.d = a.d;
   p.K = a.K;
   p.B = (uint32_t)search_buffer_capacity(a.K);
+  if (a.shape.buffer > 0 && (uint32_t)a.shape.buffer > p.B && (a.shape.buffer & (a.shape.buffer - 1)) == 0 &&
+      a.shape.buffer <= 4096)
+    p.B = (uint32_t)a.shape.buffer;
+  p.qchunk = a.shape.qchunk > 0 ? (uint32_t)a.shape.qchunk : (uint32_t)QCHUNK;
+  const int wpb = a.shape.warps_per_block;
   p.qlist = a.qlist;
   p.nq = a.nq;
   p.radius = a.radius;
@@ -770,14 +777,14 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s) {
   KNNSJ_CUDA(cudaMemsetAsync(a.work_counter, 0, sizeof(uint32_t), s));
   const bool full = a.grid.geom.di == a.d;  // every dimension indexed
   switch (a.d) {
-    case 2: full ? launch_one<T, 2, 2>(p, sm_count, s) : launch_one<T, 2, 0>(p, sm_count, s); break;
-    case 3: full ? launch_one<T, 3, 3>(p, sm_count, s) : launch_one<T, 3, 0>(p, sm_count, s); break;
-    case 4: full ? launch_one<T, 4, 4>(p, sm_count, s) : launch_one<T, 4, 0>(p, sm_count, s); break;
-    case 5: full ? launch_one<T, 5, 5>(p, sm_count, s) : launch_one<T, 5, 0>(p, sm_count, s); break;
-    case 6: full ? launch_one<T, 6, 6>(p, sm_count, s) : launch_one<T, 6, 0>(p, sm_count, s); break;
-    case 7: full ? launch_one<T, 7, 7>(p, sm_count, s) : launch_one<T, 7, 0>(p, sm_count, s); break;
-    case 8: full ? launch_one<T, 8, 8>(p, sm_count, s) : launch_one<T, 8, 0>(p, sm_count, s); break;
-    default: launch_one<T, 0, 0>(p, sm_count, s); break;
+    case 2: full ? launch_one<T, 2, 2>(p, wpb, sm_count, s) : launch_one<T, 2, 0>(p, wpb, sm_count, s); break;
+    case 3: full ? launch_one<T, 3, 3>(p, wpb, sm_count, s) : launch_one<T, 3, 0>(p, wpb, sm_count, s); break;
+    case 4: full ? launch_one<T, 4, 4>(p, wpb, sm_count, s) : launch_one<T, 4, 0>(p, wpb, sm_count, s); break;
+    case 5: full ? launch_one<T, 5, 5>(p, wpb, sm_count, s) : launch_one<T, 5, 0>(p, wpb, sm_count, s); break;
+    case 6: full ? launch_one<T, 6, 6>(p, wpb, sm_count, s) : launch_one<T, 6, 0>(p, wpb, sm_count, s); break;
+    case 7: full ? launch_one<T, 7, 7>(p, wpb, sm_count, s) : launch_one<T, 7, 0>(p, wpb, sm_count, s); break;
+    case 8: full ? launch_one<T, 8, 8>(p, wpb, sm_count, s) : launch_one<T, 8, 0>(p, wpb, sm_count, s); break;
+    default: launch_one<T, 0, 0>(p, wpb, sm_count, s); break;
   }
 }
 

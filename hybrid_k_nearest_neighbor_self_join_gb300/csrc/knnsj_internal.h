@@ -30,8 +30,9 @@ struct StatusError {
   const char* what;
 };
 
-// Kernel launches since the last reset (reported in knnsj_stats).
-extern unsigned long long g_launches;
+// Kernel launches of this host thread since the last reset (reported in
+// knnsj_stats; batched joins run sets on several host threads).
+extern thread_local unsigned long long g_launches;
 #define KNNSJ_CHECK_LAUNCH()                 \
   do {                                       \
     KNNSJ_CUDA(cudaGetLastError());          \
@@ -126,6 +127,12 @@ void launch_gather_sorted(const T* soa, uint64_t n, uint32_t d, const uint32_t* 
                           cudaStream_t s);
 
 // ---- range search with fused top-K --------------------------------------
+// Launch shape of the search kernel; 0 = the default.
+struct SearchShape {
+  int warps_per_block = 0;  // 2..8
+  int qchunk = 0;           // queries a warp takes per work fetch
+  int buffer = 0;           // selection buffer capacity (power of two >= K+32)
+};
 template <typename T>
 struct SearchLaunch {
   DeviceGrid<T> grid;
@@ -145,6 +152,7 @@ struct SearchLaunch {
   unsigned long long* cand_count = nullptr;
   uint32_t* work_counter = nullptr;
   unsigned long long* rmax_bits = nullptr;  // largest grown radius of a failure (per-query radii)
+  SearchShape shape;                        // launch shape (autotuned for batched joins)
 };
 template <typename T>
 void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s);
