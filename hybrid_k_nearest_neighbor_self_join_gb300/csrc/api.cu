@@ -49,6 +49,15 @@ knnsj_status make_config(const knnsj_options* o, uint32_t d, JoinConfig* c) {
   if (const char* e = env("KNNSJ_NUMINDEXEDDIM")) c->num_indexed_dims = (uint32_t)std::atoi(e);
   if (const char* e = env("KNNSJ_VERBOSE")) c->verbose = std::atoi(e);
   if (const char* e = env("KNNSJ_DENSE")) c->dense_mode = std::atoi(e);
+  if (const char* e = env("KNNSJ_GRAPH")) c->use_graph = std::atoi(e);
+  if (const char* e = env("KNNSJ_SEARCH_SHAPE")) {  // "warps,qchunk,buffer" (0 = default)
+    int a = 0, b = 0, bb = 0;
+    if (std::sscanf(e, "%d,%d,%d", &a, &b, &bb) >= 1) {
+      c->search_warps = a;
+      c->search_qchunk = b;
+      c->search_buffer = bb;
+    }
+  }
   if (o) {
     if (o->struct_size < sizeof(uint32_t)) return KNNSJ_ERR_INVALID_ARGUMENT;
     if (o->num_indexed_dims > 0) c->num_indexed_dims = (uint32_t)o->num_indexed_dims;

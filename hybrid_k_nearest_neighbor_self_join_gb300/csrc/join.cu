@@ -143,6 +143,7 @@ struct SmallDev {  // layout of Workspace::small
   double csum;
   double cpart[1024];
   unsigned long long rmax_bits;
+  LoopCtl ctl;
 };
 
 template <typename T>
@@ -233,6 +234,65 @@ static double ring_rows(double r, double w, uint32_t di) {
   const double per = 2.0 * r / w + 1.0;
   return std::pow(per, (double)(di > 0 ? di - 1 : 0));
 }
+
+// A grid of width w is rebuilt before a pass whose largest radius rmax needs
+// more ring rows than max(3^(di-1), 64) (and exceeds w).  The row count grows
+// with rmax, so the rule is rmax > r_limit: the largest radius that still
+// fits, found once per grid by bisection over the ordered bit patterns of
+// positive doubles.  The host loop and the graph's step kernel both use it.
+static double regrid_limit(double w, uint32_t di) {
+  const double allowed = std::max(std::pow(3.0, (double)(di - 1)), 64.0);
+  auto over = [&](double r) { return ring_rows(r, w, di) > allowed; };
+  uint64_t lo = 0, hi;  // bit patterns: over(lo) false, over(hi) true
+  double top = w;
+  while (!over(top)) top *= 2.0;
+  std::memcpy(&hi, &top, 8);
+  while (hi - lo > 1) {
+    const uint64_t mid = lo + (hi - lo) / 2;
+    double x;
+    std::memcpy(&x, &mid, 8);
+    if (over(x))
+      hi = mid;
+    else
+      lo = mid;
+  }
+  double r;
+  std::memcpy(&r, &lo, 8);
+  return r;
+}
+
+namespace {
+
+// One pass's bookkeeping inside the retry graph, mirroring the host loop of
+// run_join: count the pass, swap the lists, grow the radius, and let the next
+// pass run unless every query is done, a rebuild is due or the pass budget
+// of this graph launch is spent (the loop always ends: iter grows by one per
+// pass and stop_iter is finite).
+template <typename T>
+__global__ void loop_step_kernel(LoopCtl* c, const uint32_t* __restrict__ fail_count,
+                                 const unsigned long long* __restrict__ rmax_bits,
+                                 cudaGraphConditionalHandle handle) {
+  const uint32_t nfail = *fail_count;
+  c->queries_run += c->nq;
+  c->accepted += c->nq - nfail;
+  c->iter++;
+  c->cur ^= 1u;
+  c->nq = nfail;
+  if (nfail > 0) {
+    if (c->per_query) {
+      const unsigned long long b = *rmax_bits;
+      c->rmax = sizeof(T) == 4 ? (double)__uint_as_float((uint32_t)b) : __longlong_as_double((long long)b);
+    } else {
+      c->r = (double)(T)__dadd_rn(c->r, c->step);  // main.cu:336
+      c->rmax = c->r;
+    }
+    c->rmax_seen = fmax(c->rmax_seen, c->rmax);
+  }
+  const bool regrid = c->rmax > c->r_limit && c->rmax > c->width;
+  cudaGraphSetConditional(handle, (nfail > 0 && c->iter < c->stop_iter && !regrid) ? 1u : 0u);
+}
+
+}  // namespace
 
 // Steps 1-4 of the pipeline: dimension order, column transpose, eps0 and
 // the grid index at eps0.
@@ -374,6 +434,76 @@ static double decode_radius(unsigned long long bits) {
   return x;
 }
 
+// Runs retry passes on the device: a CUDA graph whose conditional while node
+// repeats [clear the pass counters, search, loop_step_kernel] until the step
+// kernel stops it.  c holds the loop state on entry and is updated on return.
+// Returns false, having run nothing, when conditional graph nodes are not
+// available.
+template <typename T>
+static bool run_graph_passes(SearchLaunch<T> a, LoopCtl& c, LoopCtl* dctl, SmallDev* sm, int sm_count,
+                             cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, double* kernel_ms) {
+  cudaGraph_t g = nullptr;
+  KNNSJ_CUDA(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle h;
+  if (cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+    cudaGetLastError();
+    cudaGraphDestroy(g);
+    return false;
+  }
+  // (the parameter union has no default constructor: zeroed raw storage)
+  alignas(cudaGraphNodeParams) unsigned char np_raw[sizeof(cudaGraphNodeParams)];
+  std::memset(np_raw, 0, sizeof(np_raw));
+  cudaGraphNodeParams* np = reinterpret_cast<cudaGraphNodeParams*>(np_raw);
+  np->type = cudaGraphNodeTypeConditional;
+  np->conditional.handle = h;
+  np->conditional.type = cudaGraphCondTypeWhile;
+  np->conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, np) != cudaSuccess) {
+    cudaGetLastError();
+    cudaGraphDestroy(g);
+    return false;
+  }
+  cudaGraph_t body = np->conditional.phGraph_out[0];
+  cudaGraphExec_t ex = nullptr;
+  try {
+    KNNSJ_CUDA(cudaMemcpyAsync(dctl, &c, sizeof(LoopCtl), cudaMemcpyHostToDevice, s));
+    KNNSJ_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    try {
+      a.ctl = dctl;
+      a.qlist = c.list[c.cur];  // placeholders: the kernel reads the live values from dctl
+      a.fail_list = c.list[c.cur ^ 1];
+      a.nq = c.nq;
+      KNNSJ_CUDA(cudaMemsetAsync(&sm->fail_count, 0, 4, s));
+      KNNSJ_CUDA(cudaMemsetAsync(&sm->rmax_bits, 0, 8, s));
+      launch_search<T>(a, sm_count, s);
+      loop_step_kernel<T><<<1, 1, 0, s>>>(dctl, &sm->fail_count, &sm->rmax_bits, h);
+      KNNSJ_CHECK_LAUNCH();
+    } catch (...) {
+      cudaGraph_t dummy = nullptr;
+      cudaStreamEndCapture(s, &dummy);
+      throw;
+    }
+    KNNSJ_CUDA(cudaStreamEndCapture(s, &body));
+    KNNSJ_CUDA(cudaGraphInstantiate(&ex, g, 0));
+    KNNSJ_CUDA(cudaEventRecord(e0, s));
+    KNNSJ_CUDA(cudaGraphLaunch(ex, s));
+    KNNSJ_CUDA(cudaEventRecord(e1, s));
+    KNNSJ_CUDA(cudaMemcpyAsync(&c, dctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, s));
+    KNNSJ_CUDA(cudaStreamSynchronize(s));
+  } catch (...) {
+    if (ex) cudaGraphExecDestroy(ex);
+    cudaGraphDestroy(g);
+    throw;
+  }
+  float ms = 0.f;
+  KNNSJ_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  *kernel_ms += ms;
+  cudaGraphExecDestroy(ex);
+  cudaGraphDestroy(g);
+  return true;
+}
+
 template <typename T>
 void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
               uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s) {
@@ -432,19 +562,53 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   uint64_t queries_run = 0;
   double kernel_ms = 0.0, alg_bytes = 0.0, rmax_seen = rmax;
   const int max_iter = cfg.max_iterations > 0 ? cfg.max_iterations : 100000;
+  double r_limit = regrid_limit((double)a.grid.geom.width, di);
+  // passes after the first run inside a CUDA graph (no host round trip per
+  // pass) unless the stream cannot be captured (the legacy default stream)
+  bool graph_ok = cfg.use_graph && s != nullptr && ev[4] != nullptr;
+  LoopCtl* dctl = &sm->ctl;
   while (nq > 0) {
     if (iter >= max_iter) throw StatusError{KNNSJ_ERR_NO_CONVERGENCE, "iteration cap reached"};
-    const double rows = ring_rows(rmax, (double)a.grid.geom.width, di);
-    const double allowed = std::max(std::pow(3.0, (double)(di - 1)), 64.0);
     // learned starting radii are clamped so their rings stay small on the
     // eps0 grid: no rebuild for the first pass
     const bool first_learned = qrad && iter == 0;
-    if (!first_learned && rows > allowed && rmax > (double)a.grid.geom.width) {
+    if (!first_learned && rmax > r_limit && rmax > (double)a.grid.geom.width) {
       // coarser grid for the largest radius in flight (like main.cu:333-356);
       // the widened width keeps its ring at three cells per dimension
       const T wnew = (T)(rmax * (1.0 + 1.0 / 32768.0));
       build_grid<T>(w, cfg, n, d, di, P.mn, P.mx, wnew, &a.grid, s);
+      r_limit = regrid_limit((double)a.grid.geom.width, di);
       regrids++;
+    }
+    if (graph_ok && iter >= 1) {
+      LoopCtl c{};
+      c.nq = nq;
+      c.iter = (uint32_t)iter;
+      c.cur = (uint32_t)cur;
+      c.stop_iter = (uint32_t)std::min<int64_t>((int64_t)max_iter, (int64_t)iter + 256);
+      c.list[0] = list[0];
+      c.list[1] = list[1];
+      c.r = (double)r;
+      c.step = step;
+      c.rmax = rmax;
+      c.rmax_seen = rmax_seen;
+      c.r_limit = r_limit;
+      c.width = (double)a.grid.geom.width;
+      c.per_query = qrad ? 1 : 0;
+      if (run_graph_passes<T>(a, c, dctl, sm, w.sm_count, s, ev[4], ev[5], &kernel_ms)) {
+        const int passes = (int)c.iter - iter;
+        alg_bytes += (double)passes * n * d * sizeof(T) + (double)c.queries_run * d * sizeof(T) +
+                     (double)c.accepted * K * (4.0 + sizeof(T));
+        queries_run += c.queries_run;
+        iter = (int)c.iter;
+        cur = (int)c.cur;
+        nq = c.nq;
+        r = (T)c.r;
+        rmax = c.rmax;
+        rmax_seen = c.rmax_seen;
+        continue;
+      }
+      graph_ok = false;  // conditional graphs unavailable: host-driven passes
     }
     a.qlist = iter == 0 ? nullptr : list[cur];
     a.nq = nq;

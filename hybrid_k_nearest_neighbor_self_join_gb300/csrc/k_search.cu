@@ -101,6 +101,7 @@ struct SearchParams {
   uint32_t qchunk;
   const uint32_t* __restrict__ qlist;
   uint32_t nq;
+  const LoopCtl* ctl;
   T radius;
   T* qradius;
   double step;
@@ -422,19 +423,41 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search
   const uint32_t K = p.K;
   const uint32_t B = p.B;
   unsigned long long scanned = 0;
+  // the pass's queries, failure list and radius: from the launch, or from
+  // the loop state when the pass runs inside the retry graph (kept in shared
+  // memory, not in registers, which the scan loop needs)
+  __shared__ uint32_t s_nq;
+  __shared__ const uint32_t* s_qlist;
+  __shared__ uint32_t* s_fail;
+  __shared__ T s_radius;
+  if (threadIdx.x == 0) {
+    if (p.ctl) {
+      s_nq = p.ctl->nq;
+      s_qlist = p.ctl->list[p.ctl->cur];
+      s_fail = p.ctl->list[p.ctl->cur ^ 1];
+      s_radius = (T)p.ctl->r;
+    } else {
+      s_nq = p.nq;
+      s_qlist = p.qlist;
+      s_fail = p.fail_list;
+      s_radius = p.radius;
+    }
+  }
+  __syncthreads();
 
   for (;;) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(p.work_counter, p.qchunk);
     base = __shfl_sync(FULL, base, 0);
-    if (base >= p.nq) break;
-    const uint32_t qend = min(base + p.qchunk, p.nq);
+    if (base >= s_nq) break;
+    const uint32_t qend = min(base + p.qchunk, s_nq);
     for (uint32_t qi = base; qi < qend; ++qi) {
       // first pass: every point in cell order; later passes: the failed
       // queries by original id (valid across grid rebuilds)
-      const uint32_t qid = p.qlist ? p.qlist[qi] : p.pid[qi];
-      const T* qsrc = p.qlist ? p.xs : p.ps;
-      const uint32_t qcol = p.qlist ? qid : qi;
+      const uint32_t* qlist = s_qlist;
+      const uint32_t qid = qlist ? qlist[qi] : p.pid[qi];
+      const T* qsrc = qlist ? p.xs : p.ps;
+      const uint32_t qcol = qlist ? qid : qi;
       T q[D > 0 ? D : 1];
       if (D > 0) {
 #pragma unroll
@@ -444,7 +467,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search
         __syncwarp();
       }
       auto qdim = [&](int j) -> T { return (D > 0) ? q[j < D ? j : 0] : qsm[j]; };
-      const T r = p.qradius ? p.qradius[qid] : p.radius;
+      const T r = p.qradius ? p.qradius[qid] : s_radius;
       const T thr = within_threshold(r);
 
       // All bound arithmetic below is float, widened by explicit slack so
@@ -693,7 +716,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search
         }
       } else if (lane == 0) {
         const uint32_t slot = atomicAdd(p.fail_count, 1u);
-        p.fail_list[slot] = qid;
+        s_fail[slot] = qid;
         if (p.qradius) {
           // the plain BETA schedule from the learned start: grow by eps0/2
           const T rn = (T)((double)r + p.step);
@@ -724,7 +747,9 @@ void launch_one(const SearchParams<T>& prm, int wpb_req, int sm_count, cudaStrea
   const uint64_t warps_needed = (prm.nq + prm.qchunk - 1) / prm.qchunk;
   uint64_t blocks = (uint64_t)per_sm * sm_count;
   const uint64_t need_blocks = (warps_needed + wpb - 1) / wpb;
-  if (need_blocks < blocks) blocks = need_blocks;
+  // inside the retry graph the pass size is known only on the device: the
+  // full persistent grid, whose surplus warps find no work and leave
+  if (!prm.ctl && need_blocks < blocks) blocks = need_blocks;
   if (blocks < 1) blocks = 1;
   kern<<<(unsigned)blocks, wpb * 32, smem, s>>>(prm);
   KNNSJ_CHECK_LAUNCH();
@@ -764,6 +789,7 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s) {
   const int wpb = a.shape.warps_per_block;
   p.qlist = a.qlist;
   p.nq = a.nq;
+  p.ctl = a.ctl;
   p.radius = a.radius;
   p.qradius = a.qradius;
   p.step = (double)a.step;

@@ -127,6 +127,28 @@ void launch_gather_sorted(const T* soa, uint64_t n, uint32_t d, const uint32_t* 
                           cudaStream_t s);
 
 // ---- range search with fused top-K --------------------------------------
+// State of the retry loop in device memory, for passes that run inside a
+// CUDA graph (a conditional while node): the search kernel reads the pass's
+// query count, lists and radius from here, and a one-thread step kernel
+// advances it and decides whether another pass runs.
+struct LoopCtl {
+  uint32_t nq;         // queries of the next pass
+  uint32_t iter;       // passes done
+  uint32_t cur;        // list[cur] holds the next pass's queries
+  uint32_t stop_iter;  // the graph stops before this pass
+  uint32_t* list[2];
+  double r;            // uniform radius (a value of the data type)
+  double step;         // radius growth per pass
+  double rmax;         // largest radius the next pass searches
+  double rmax_seen;    // largest radius of any pass
+  double r_limit;      // a grid rebuild is due when rmax > r_limit and rmax > width
+  double width;
+  unsigned long long queries_run;
+  unsigned long long accepted;
+  int per_query;       // per-query radii (learned starting radius)
+  int pad;
+};
+
 // Launch shape of the search kernel; 0 = the default.
 struct SearchShape {
   int warps_per_block = 0;  // 2..8
@@ -153,6 +175,7 @@ struct SearchLaunch {
   uint32_t* work_counter = nullptr;
   unsigned long long* rmax_bits = nullptr;  // largest grown radius of a failure (per-query radii)
   SearchShape shape;                        // launch shape (autotuned for batched joins)
+  const LoopCtl* ctl = nullptr;             // non-null: nq, lists and radius come from here (graph passes)
 };
 template <typename T>
 void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s);

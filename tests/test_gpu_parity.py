@@ -121,6 +121,22 @@ def test_dense_and_sparse_cell_lookup_agree(monkeypatch):
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
 
 
+@pytest.mark.parametrize("mode", [kj.RADIUS_PLAIN, kj.RADIUS_LEARNED])
+def test_graph_passes_match_host_passes(monkeypatch, mode):
+    # retry passes inside the conditional CUDA graph against host-driven
+    # passes: same rows, same pass count, rebuilds and candidates
+    x = datasets.gmm(200_000, 4, 30, 0.2, 21, dtype=np.float32)
+    out = {}
+    for g in ("0", "1"):
+        monkeypatch.setenv("KNNSJ_GRAPH", g)
+        out[g] = kj.selfjoin(x, 32, beta=0.0, radius_mode=mode, return_stats=True)
+    (a_i, a_d, a_s), (b_i, b_d, b_s) = out["0"], out["1"]
+    assert np.array_equal(a_i, b_i) and np.array_equal(a_d, b_d)
+    assert a_s["iterations"] > 2
+    for key in ("iterations", "regrids", "candidates", "queries_run", "eps_final"):
+        assert a_s[key] == b_s[key], key
+
+
 def test_tiny_input_eps_fallback():
     # N <= 1000: the reference's sampled mean distance is 0 and its grid
     # divides by zero; the GPU path picks a positive width and stays exact.
