@@ -43,8 +43,8 @@ namespace {
 
 constexpr int SEARCH_THREADS = 256;  // largest block; the launch may use fewer warps
 constexpr int QCHUNK = 4;            // default queries per work fetch
-// ring rows per wave (each gives at most two runs of points): for one or two
-// indexed dimensions, and for more (wider rings of shorter rows)
+// ring rows per wave (each row is one run of points): for one or two indexed
+// dimensions, and for more (wider rings of shorter rows)
 #ifndef KNNSJ_WAVE_ROWS_LO
 #define KNNSJ_WAVE_ROWS_LO 16
 #endif
@@ -74,7 +74,7 @@ constexpr int QCHUNK = 4;            // default queries per work fetch
 #define KNNSJ_TIGHTEN 2
 #endif
 constexpr int MAX_WAVE_ROWS = KNNSJ_WAVE_ROWS_LO > KNNSJ_WAVE_ROWS_HI ? KNNSJ_WAVE_ROWS_LO : KNNSJ_WAVE_ROWS_HI;
-constexpr int MAX_RUNS = 2 * MAX_WAVE_ROWS;
+constexpr int MAX_RUNS = MAX_WAVE_ROWS;  // one run of points per row
 static_assert(MAX_WAVE_ROWS <= 32, "a wave is at most one row per lane");
 template <int DI>
 constexpr int wave_rows() {
@@ -387,21 +387,21 @@ __device__ __forceinline__ unsigned long long warp_sort32(unsigned long long v, 
 }
 
 // resident blocks per SM the register budget is cut for: low dimensions
-// (d <= 3) fit 64 registers without spilling, higher ones need more
+// (d <= 3, all indexed) fit 64 registers, higher ones need more
 #ifndef KNNSJ_MINB_LO
 #define KNNSJ_MINB_LO 4
 #endif
 #ifndef KNNSJ_MINB_HI
 #define KNNSJ_MINB_HI 3
 #endif
-template <int D>
+template <int D, int DI>
 constexpr int search_min_blocks() {
-  return (D > 0 && D <= 3) ? KNNSJ_MINB_LO : KNNSJ_MINB_HI;
+  return (D > 0 && D <= 3 && DI > 0) ? KNNSJ_MINB_LO : KNNSJ_MINB_HI;
 }
 
 // D: data dimensions (0 = runtime); DI: indexed dimensions (0 = runtime, <= MAX_DI).
 template <typename T, int D, int DI>
-__global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search_kernel(const SearchParams<T> p) {
+__global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D, DI>()) search_kernel(const SearchParams<T> p) {
   constexpr int WAVE_ROWS = wave_rows<DI>();
   constexpr int NDI = DI > 0 ? DI : MAX_DI;
   using Kt = Key<T>;
@@ -476,11 +476,11 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search
       // Cell ring: a point whose computed squared distance is <= thr differs
       // from the query by at most r * (1 + 2^-16) per coordinate.
       const float rf = to_float_up(r) * (1.0f + 1.0f / 8192.0f);
-      uint32_t lo[NDI], hi[NDI], own[NDI], magic[NDI];
+      uint32_t lo[NDI], hi[NDI], magic[NDI];
       float qf[NDI];
 #pragma unroll
       for (int j = 0; j < NDI; j++) {
-        lo[j] = hi[j] = own[j] = magic[j] = 0;
+        lo[j] = hi[j] = magic[j] = 0;
         qf[j] = 0.0f;
         if (j < (int)di) {
           const T qj = qdim(j);
@@ -488,8 +488,6 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search
           const float slack = (fabsf(qf[j]) + rf) * (1.0f / 2097152.0f);
           lo[j] = clamped_cell((T)(qf[j] - rf - slack), p.g.minv[j], p.g.width, p.g.ncell[j]);
           hi[j] = clamped_cell((T)(qf[j] + rf + slack), p.g.minv[j], p.g.width, p.g.ncell[j]);
-          const uint32_t c = clamped_cell(qj, p.g.minv[j], p.g.width, p.g.ncell[j]);
-          own[j] = c < lo[j] ? lo[j] : (c > hi[j] ? hi[j] : c);
           const uint32_t ext = hi[j] - lo[j] + 1;
           magic[j] = ext > 1 ? 0xffffffffu / ext + 1u : 0u;  // x / ext == umulhi(x, magic) for small x
         }
@@ -500,15 +498,13 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search
         if (j < (int)di) nrows *= (unsigned long long)(hi[j] - lo[j] + 1);
       const float wf = (float)p.g.width;
 
-      // Row ridx of the ring: linear id of its dimension-0 origin, whether it
-      // is the query's own row, and a lower bound of the computed squared
-      // distance of any of its points (dimensions 1..di-1, less 2^-14 for
-      // the rounding of the distance itself).
-      auto row_info = [&](uint32_t ridx, unsigned long long& rbase, bool& center) -> float {
+      // Row ridx of the ring: linear id of its dimension-0 origin and a lower
+      // bound of the computed squared distance of any of its points
+      // (dimensions 1..di-1, less 2^-14 for the rounding of the distance).
+      auto row_info = [&](uint32_t ridx, unsigned long long& rbase) -> float {
         uint32_t rem = ridx;
         unsigned long long lin = 0;
         float lbf = 0.0f;
-        center = true;
 #pragma unroll
         for (int j = 1; j < NDI; j++) {
           if (j < (int)di) {
@@ -525,7 +521,6 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search
             rem = qq;
             const uint32_t c = lo[j] + (uint32_t)rj;
             lin += (unsigned long long)c * p.g.mult[j];
-            center = center && (c == own[j]);
             const float mv = (float)p.g.minv[j];
             const float slo = mv + (float)c * wf;
             const float shi = slo + wf;
@@ -542,17 +537,22 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search
       st.len = 0;
       st.tau = Kt::bound(thr);
       st.tight = false;
+      // a uniform radius tightens the threshold after each wave (the first
+      // wave being the query's own row alone), so rows are visited nearest
+      // first; per-query radii are already close to the K-th distance
+      const bool tighten = KNNSJ_TIGHTEN == 1 || (KNNSJ_TIGHTEN == 2 && p.qradius == nullptr);
+      const bool sorted_rows = KNNSJ_SORT_ROWS && (nrows > KNNSJ_SORT_MIN_ROWS || (tighten && nrows > 1));
 
       bool fail_now = false;
-      if (KNNSJ_EARLY_FAIL && p.dense) {
+      if (KNNSJ_EARLY_FAIL && p.dense && nrows > 32) {
         // fewer than K points in the whole ring: this radius cannot succeed
+        // (rings of one group are counted from the runs loaded below)
         uint32_t cnt = 0;
         for (unsigned long long g0 = 0; g0 < nrows; g0 += 32) {
           const unsigned long long ridx = g0 + lane;
           if (ridx < nrows) {
             unsigned long long rb;
-            bool cen;
-            row_info((uint32_t)ridx, rb, cen);
+            row_info((uint32_t)ridx, rb);
             cnt += p.dstart[rb + hi[0] + 1] - p.dstart[rb + lo[0]];
           }
         }
@@ -561,108 +561,101 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D>()) search
         fail_now = cnt < K;
       }
 
-      // Producer of run lists: first the query's own cell, then the other
-      // rows of the ring in groups of 32 sorted by lower bound, a wave of
-      // WAVE_ROWS rows at a time.  One scan loop consumes them all.
-      bool own_pending = !fail_now;
-      const bool sorted_rows = KNNSJ_SORT_ROWS && nrows > KNNSJ_SORT_MIN_ROWS;
-      const bool tighten = KNNSJ_TIGHTEN == 1 || (KNNSJ_TIGHTEN == 2 && p.qradius == nullptr);
-      unsigned long long g0 = 0;   // first row of the current group
-      int nvalid = 0, w0 = 0;      // rows in the group, next wave start
+      // Producer of run lists: the rows of the ring in groups of 32, each
+      // lane loading its row's full dimension-0 run (one memory round trip
+      // per group), sorted by lower bound when that can prune, consumed a
+      // wave of rows at a time; a row is cut to a narrower run only once K
+      // keys are held.  One scan loop consumes the runs.
+      unsigned long long g0 = 0;  // first row of the current group
+      int nvalid = 0, w0 = 0;     // rows in the group, next wave start
       unsigned long long skey = 0, rbase = 0;
-      bool rcenter = false;
+      uint32_t rs = 0, re = 0;    // this lane's row of the group: its full run
+      bool first_wave = true;
       const unsigned long long groups_end = fail_now ? 0 : nrows;
       for (;;) {
         uint32_t total = 0;
         int nr = 1;
-        if (own_pending) {
-          own_pending = false;
-          unsigned long long Lown = 0;
+        if (w0 >= nvalid) {  // next group of rows
+          if (nvalid > 0) g0 += 32;
+          if (g0 >= groups_end) break;
+          const unsigned long long ridx = g0 + lane;
+          float rlb = __int_as_float(0x7f800000);
+          rbase = 0;
+          rs = re = 0;
+          if (ridx < nrows) {
+            rlb = row_info((uint32_t)ridx, rbase);
+            run_of(p, rbase + lo[0], rbase + hi[0], rs, re);
+          }
+          if (KNNSJ_EARLY_FAIL && nrows <= 32) {
+            uint32_t cnt = re - rs;
 #pragma unroll
-          for (int j = 0; j < NDI; j++)
-            if (j < (int)di) Lown += (unsigned long long)own[j] * p.g.mult[j];
-          uint32_t s_own, e_own;
-          run_of(p, Lown, Lown, s_own, e_own);
-          if (lane == 0) {
-            runS[0] = s_own;
-            runP[0] = 0;
+            for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(FULL, cnt, off);
+            if (cnt < K) break;  // the whole ring holds fewer than K points
           }
-          total = e_own - s_own;
-        } else {
-          if (w0 >= nvalid) {  // next group of rows
-            if (nvalid > 0) g0 += 32;
-            if (g0 >= groups_end) break;
-            const unsigned long long ridx = g0 + lane;
-            float rlb = __int_as_float(0x7f800000);
-            rbase = 0;
-            rcenter = false;
-            if (ridx < nrows) rlb = row_info((uint32_t)ridx, rbase, rcenter);
-            skey = ((unsigned long long)__float_as_uint(rlb) << 32) | (unsigned long long)(uint32_t)lane;
-            if (sorted_rows) skey = warp_sort32(skey, lane);
-            nvalid = (int)min(32ull, nrows - g0);
-            w0 = 0;
-          }
-          const unsigned long long myk = __shfl_sync(FULL, skey, (w0 + lane) & 31);
-          const int srcl = (int)(myk & 31u);
-          const unsigned long long lb = __shfl_sync(FULL, rbase, srcl);
-          const bool center = __shfl_sync(FULL, (int)rcenter, srcl) != 0;
-          const float lbs = __uint_as_float((uint32_t)(myk >> 32));
-          const bool active = lane < WAVE_ROWS && w0 + lane < nvalid;
-          const float tup = to_float_up(Kt::acc(st.tau));
-          const bool have = st.len >= K;
-          // rows come in ascending lower bound: the rest of the group can go
-          const float first_lb = __shfl_sync(FULL, lbs, 0);
-          if (sorted_rows && have && first_lb > tup) {
-            w0 = nvalid;
-            continue;
-          }
-          uint32_t sA = 0, eA = 0, sB = 0, eB = 0;
-          if (active) {
-            uint32_t xl = lo[0], xh = hi[0];
-            bool empty = false;
-            if (have) {
-              if (lbs > tup) {
-                empty = true;
-              } else {
-                // dimension-0 interval that can still hold a better point
-                const float avail = tup * (1.0f + 1.0f / 16384.0f) - lbs;
-                const float g = sqrtf(fmaxf(avail, 0.0f)) * (1.0f + 1.0f / 1048576.0f);
-                const float slack = (fabsf(qf[0]) + g) * (1.0f / 2097152.0f);
-                const uint32_t a0 = clamped_cell((T)(qf[0] - g - slack), p.g.minv[0], p.g.width, p.g.ncell[0]);
-                const uint32_t b0 = clamped_cell((T)(qf[0] + g + slack), p.g.minv[0], p.g.width, p.g.ncell[0]);
-                xl = max(xl, a0);
-                xh = min(xh, b0);
-                empty = xl > xh;
-              }
-            }
-            if (!empty) {
-              if (center) {
-                // the own cell was scanned first
-                if (own[0] > xl) run_of(p, lb + xl, lb + own[0] - 1, sA, eA);
-                if (own[0] < xh) run_of(p, lb + own[0] + 1, lb + xh, sB, eB);
-              } else {
-                run_of(p, lb + xl, lb + xh, sA, eA);
-              }
-            }
-          }
-          const uint32_t la = eA - sA, lbn = eB - sB;
-          uint32_t incl = la + lbn;
-#pragma unroll
-          for (int off = 1; off < 32; off <<= 1) {
-            const uint32_t t = __shfl_up_sync(FULL, incl, off);
-            if (lane >= off) incl += t;
-          }
-          total = __shfl_sync(FULL, incl, WAVE_ROWS - 1);
-          if (lane < WAVE_ROWS) {
-            const uint32_t ex = incl - la - lbn;
-            runS[2 * lane] = sA;
-            runS[2 * lane + 1] = sB;
-            runP[2 * lane] = ex;
-            runP[2 * lane + 1] = ex + la;
-          }
-          nr = 2 * WAVE_ROWS;
-          w0 += WAVE_ROWS;
+          skey = ((unsigned long long)__float_as_uint(rlb) << 32) | (unsigned long long)(uint32_t)lane;
+          if (sorted_rows) skey = warp_sort32(skey, lane);
+          nvalid = (int)min(32ull, nrows - g0);
+          w0 = 0;
         }
+        const int wave = (tighten && first_wave) ? 1 : WAVE_ROWS;
+        first_wave = false;
+        const unsigned long long myk = __shfl_sync(FULL, skey, (w0 + lane) & 31);
+        const int srcl = (int)(myk & 31u);
+        const unsigned long long lb = __shfl_sync(FULL, rbase, srcl);
+        const uint32_t s0 = __shfl_sync(FULL, rs, srcl);
+        const uint32_t e0 = __shfl_sync(FULL, re, srcl);
+        const float lbs = __uint_as_float((uint32_t)(myk >> 32));
+        const bool active = lane < wave && w0 + lane < nvalid;
+        const float tup = to_float_up(Kt::acc(st.tau));
+        const bool have = st.len >= K;
+        // rows come in ascending lower bound: the rest of the group can go
+        const float first_lb = __shfl_sync(FULL, lbs, 0);
+        if (sorted_rows && have && first_lb > tup) {
+          w0 = nvalid;
+          continue;
+        }
+        uint32_t sA = 0, eA = 0;
+        if (active) {
+          uint32_t xl = lo[0], xh = hi[0];
+          bool empty = false;
+          if (have) {
+            if (lbs > tup) {
+              empty = true;
+            } else {
+              // dimension-0 interval that can still hold a better point
+              const float avail = tup * (1.0f + 1.0f / 16384.0f) - lbs;
+              const float g = sqrtf(fmaxf(avail, 0.0f)) * (1.0f + 1.0f / 1048576.0f);
+              const float slack = (fabsf(qf[0]) + g) * (1.0f / 2097152.0f);
+              const uint32_t a0 = clamped_cell((T)(qf[0] - g - slack), p.g.minv[0], p.g.width, p.g.ncell[0]);
+              const uint32_t b0 = clamped_cell((T)(qf[0] + g + slack), p.g.minv[0], p.g.width, p.g.ncell[0]);
+              xl = max(xl, a0);
+              xh = min(xh, b0);
+              empty = xl > xh;
+            }
+          }
+          if (!empty) {
+            if (xl == lo[0] && xh == hi[0]) {
+              sA = s0;
+              eA = e0;
+            } else {
+              run_of(p, lb + xl, lb + xh, sA, eA);
+            }
+          }
+        }
+        const uint32_t la = eA - sA;
+        uint32_t incl = la;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const uint32_t t = __shfl_up_sync(FULL, incl, off);
+          if (lane >= off) incl += t;
+        }
+        total = __shfl_sync(FULL, incl, WAVE_ROWS - 1);
+        if (lane < WAVE_ROWS) {
+          runS[lane] = sA;
+          runP[lane] = incl - la;
+        }
+        nr = WAVE_ROWS;
+        w0 += wave;
         __syncwarp();
         // the scan: one squared distance per lane, ballot-append under tau
         int row = 0;
