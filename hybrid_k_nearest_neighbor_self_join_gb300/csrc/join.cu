@@ -142,7 +142,7 @@ struct SmallDev {  // layout of Workspace::small
   uint32_t hist[10000];
   double csum;
   double cpart[1024];
-  unsigned long long rmax_bits;
+  FailRadii fr;
   LoopCtl ctl;
 };
 
@@ -261,6 +261,21 @@ static double regrid_limit(double w, uint32_t di) {
   return r;
 }
 
+// The radius a rebuilt grid is sized for when queries carry their own radii:
+// the median grown radius of the failed queries (bin upper edge, at most the
+// largest), so that most of them search small rings; the few with far larger
+// radii search wider rings of the same grid.
+__host__ __device__ inline double median_fail_radius(const uint32_t* hist, uint32_t nfail, const double* redge,
+                                                     double rmax) {
+  const uint32_t target = (nfail + 1) / 2;
+  uint32_t cum = 0;
+  for (int b = 0; b < FAIL_RADIUS_BINS; b++) {
+    cum += hist[b];
+    if (cum >= target) return redge[b] < rmax ? redge[b] : rmax;
+  }
+  return rmax;
+}
+
 namespace {
 
 // One pass's bookkeeping inside the retry graph, mirroring the host loop of
@@ -270,8 +285,7 @@ namespace {
 // pass and stop_iter is finite).
 template <typename T>
 __global__ void loop_step_kernel(LoopCtl* c, const uint32_t* __restrict__ fail_count,
-                                 const unsigned long long* __restrict__ rmax_bits,
-                                 cudaGraphConditionalHandle handle) {
+                                 const FailRadii* __restrict__ fr, cudaGraphConditionalHandle handle) {
   const uint32_t nfail = *fail_count;
   c->queries_run += c->nq;
   c->accepted += c->nq - nfail;
@@ -280,15 +294,17 @@ __global__ void loop_step_kernel(LoopCtl* c, const uint32_t* __restrict__ fail_c
   c->nq = nfail;
   if (nfail > 0) {
     if (c->per_query) {
-      const unsigned long long b = *rmax_bits;
+      const unsigned long long b = fr->rmax_bits;
       c->rmax = sizeof(T) == 4 ? (double)__uint_as_float((uint32_t)b) : __longlong_as_double((long long)b);
+      c->rgrid = median_fail_radius(fr->hist, nfail, c->redge, c->rmax);
     } else {
       c->r = (double)(T)__dadd_rn(c->r, c->step);  // main.cu:336
       c->rmax = c->r;
+      c->rgrid = c->r;
     }
     c->rmax_seen = fmax(c->rmax_seen, c->rmax);
   }
-  const bool regrid = c->rmax > c->r_limit && c->rmax > c->width;
+  const bool regrid = c->rgrid > c->r_limit && c->rgrid > c->width;
   cudaGraphSetConditional(handle, (nfail > 0 && c->iter < c->stop_iter && !regrid) ? 1u : 0u);
 }
 
@@ -475,9 +491,9 @@ static bool run_graph_passes(SearchLaunch<T> a, LoopCtl& c, LoopCtl* dctl, Small
       a.fail_list = c.list[c.cur ^ 1];
       a.nq = c.nq;
       KNNSJ_CUDA(cudaMemsetAsync(&sm->fail_count, 0, 4, s));
-      KNNSJ_CUDA(cudaMemsetAsync(&sm->rmax_bits, 0, 8, s));
+      KNNSJ_CUDA(cudaMemsetAsync(&sm->fr, 0, sizeof(FailRadii), s));
       launch_search<T>(a, sm_count, s);
-      loop_step_kernel<T><<<1, 1, 0, s>>>(dctl, &sm->fail_count, &sm->rmax_bits, h);
+      loop_step_kernel<T><<<1, 1, 0, s>>>(dctl, &sm->fail_count, &sm->fr, h);
       KNNSJ_CHECK_LAUNCH();
     } catch (...) {
       cudaGraph_t dummy = nullptr;
@@ -549,7 +565,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   a.fail_count = &sm->fail_count;
   a.cand_count = &sm->cand;
   a.work_counter = &sm->work_counter;
-  a.rmax_bits = &sm->rmax_bits;
+  a.fail_radii = &sm->fr;
   a.qradius = qrad;
   a.shape.warps_per_block = cfg.search_warps;
   a.shape.qchunk = cfg.search_qchunk;
@@ -561,21 +577,24 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   int iter = 0, regrids = 0, cur = 0;
   uint64_t queries_run = 0;
   double kernel_ms = 0.0, alg_bytes = 0.0, rmax_seen = rmax;
+  double rgrid = rmax;  // the radius a rebuilt grid is sized for
+  double redge[FAIL_RADIUS_BINS];
+  for (int b = 0; b < FAIL_RADIUS_BINS; b++) redge[b] = (double)P.eps0 * std::exp2((b - 15) / 4.0);
   const int max_iter = cfg.max_iterations > 0 ? cfg.max_iterations : 100000;
   double r_limit = regrid_limit((double)a.grid.geom.width, di);
   // passes after the first run inside a CUDA graph (no host round trip per
   // pass) unless the stream cannot be captured (the legacy default stream)
-  bool graph_ok = cfg.use_graph && s != nullptr && ev[4] != nullptr;
+  bool graph_ok = cfg.use_graph && s != nullptr && ev[4] != nullptr && cfg.verbose < 2;
   LoopCtl* dctl = &sm->ctl;
   while (nq > 0) {
     if (iter >= max_iter) throw StatusError{KNNSJ_ERR_NO_CONVERGENCE, "iteration cap reached"};
     // learned starting radii are clamped so their rings stay small on the
     // eps0 grid: no rebuild for the first pass
     const bool first_learned = qrad && iter == 0;
-    if (!first_learned && rmax > r_limit && rmax > (double)a.grid.geom.width) {
-      // coarser grid for the largest radius in flight (like main.cu:333-356);
-      // the widened width keeps its ring at three cells per dimension
-      const T wnew = (T)(rmax * (1.0 + 1.0 / 32768.0));
+    if (!first_learned && rgrid > r_limit && rgrid > (double)a.grid.geom.width) {
+      // coarser grid for the radius in flight (like main.cu:333-356); the
+      // widened width keeps that radius's ring at three cells per dimension
+      const T wnew = (T)(rgrid * (1.0 + 1.0 / 32768.0));
       build_grid<T>(w, cfg, n, d, di, P.mn, P.mx, wnew, &a.grid, s);
       r_limit = regrid_limit((double)a.grid.geom.width, di);
       regrids++;
@@ -591,12 +610,16 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
       c.r = (double)r;
       c.step = step;
       c.rmax = rmax;
+      c.rgrid = rgrid;
       c.rmax_seen = rmax_seen;
+      for (int b = 0; b < FAIL_RADIUS_BINS; b++) c.redge[b] = redge[b];
       c.r_limit = r_limit;
       c.width = (double)a.grid.geom.width;
       c.per_query = qrad ? 1 : 0;
       if (run_graph_passes<T>(a, c, dctl, sm, w.sm_count, s, ev[4], ev[5], &kernel_ms)) {
         const int passes = (int)c.iter - iter;
+        // the capture counted the search and step kernels once; each pass ran both
+        g_launches += 2ull * (unsigned long long)passes - 2ull;
         alg_bytes += (double)passes * n * d * sizeof(T) + (double)c.queries_run * d * sizeof(T) +
                      (double)c.accepted * K * (4.0 + sizeof(T));
         queries_run += c.queries_run;
@@ -605,6 +628,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
         nq = c.nq;
         r = (T)c.r;
         rmax = c.rmax;
+        rgrid = c.rgrid;
         rmax_seen = c.rmax_seen;
         continue;
       }
@@ -615,20 +639,28 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     a.radius = r;
     a.fail_list = list[cur ^ 1];
     KNNSJ_CUDA(cudaMemsetAsync(&sm->fail_count, 0, 4, s));
-    KNNSJ_CUDA(cudaMemsetAsync(&sm->rmax_bits, 0, 8, s));
+    KNNSJ_CUDA(cudaMemsetAsync(&sm->fr, 0, sizeof(FailRadii), s));
     rec(4);
     launch_search<T>(a, w.sm_count, s);
     rec(5);
     struct {
       uint32_t fail;
       uint32_t pad;
-      unsigned long long rbits;
+      FailRadii fr;
     } tail;
     KNNSJ_CUDA(cudaMemcpyAsync(&tail.fail, &sm->fail_count, 4, cudaMemcpyDeviceToHost, s));
-    KNNSJ_CUDA(cudaMemcpyAsync(&tail.rbits, &sm->rmax_bits, 8, cudaMemcpyDeviceToHost, s));
+    if (qrad) KNNSJ_CUDA(cudaMemcpyAsync(&tail.fr, &sm->fr, sizeof(FailRadii), cudaMemcpyDeviceToHost, s));
     KNNSJ_CUDA(cudaStreamSynchronize(s));
     const uint32_t nfail = tail.fail;
-    kernel_ms += elapsed(4, 5);
+    const float pass_ms = elapsed(4, 5);
+    kernel_ms += pass_ms;
+    if (cfg.verbose >= 2) {  // one line per pass
+      unsigned long long cand_now = 0;
+      KNNSJ_CUDA(cudaMemcpy(&cand_now, &sm->cand, 8, cudaMemcpyDeviceToHost));
+      fprintf(stderr, "knnsj: pass %d: %u queries, %u failed, radius %g (largest %g), grid width %g, %.3f ms, "
+              "candidates so far %llu\n", iter, nq, nfail, (double)r, rmax, (double)a.grid.geom.width, pass_ms,
+              cand_now);
+    }
     // candidate columns read once, query rows read, accepted rows written
     alg_bytes += (double)n * d * sizeof(T) + (double)nq * d * sizeof(T) +
                  (double)(nq - nfail) * K * (4.0 + sizeof(T));
@@ -638,10 +670,12 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     iter++;
     if (nq > 0) {
       if (qrad) {
-        rmax = decode_radius<T>(tail.rbits);  // largest grown radius among the failures
+        rmax = decode_radius<T>(tail.fr.rmax_bits);  // largest grown radius among the failures
+        rgrid = median_fail_radius(tail.fr.hist, nfail, redge, rmax);
       } else {
         r = (T)((double)r + step);  // main.cu:336
         rmax = (double)r;
+        rgrid = rmax;
       }
       rmax_seen = std::max(rmax_seen, rmax);
     }

@@ -70,6 +70,11 @@ constexpr int QCHUNK = 4;            // default queries per work fetch
 #ifndef KNNSJ_PRE_WRITE_REDUCE
 #define KNNSJ_PRE_WRITE_REDUCE 0
 #endif
+// per-query radii of failed queries grow toward K points from the count
+// they found (1) or by eps0/2 per pass like the plain schedule (0)
+#ifndef KNNSJ_GUIDED_GROWTH
+#define KNNSJ_GUIDED_GROWTH 1
+#endif
 #ifndef KNNSJ_TIGHTEN
 #define KNNSJ_TIGHTEN 2
 #endif
@@ -111,7 +116,7 @@ struct SearchParams {
   uint32_t* fail_count;
   unsigned long long* cand_count;
   uint32_t* work_counter;
-  unsigned long long* rmax_bits;
+  FailRadii* fail_radii;
 };
 
 __device__ __forceinline__ unsigned long long lower_bound_u64(const unsigned long long* __restrict__ a,
@@ -544,6 +549,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D, DI>()) se
       const bool sorted_rows = KNNSJ_SORT_ROWS && (nrows > KNNSJ_SORT_MIN_ROWS || (tighten && nrows > 1));
 
       bool fail_now = false;
+      uint32_t ring_cnt = 0;  // points in the ring's cells, when counted
       if (KNNSJ_EARLY_FAIL && p.dense && nrows > 32) {
         // fewer than K points in the whole ring: this radius cannot succeed
         // (rings of one group are counted from the runs loaded below)
@@ -559,6 +565,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D, DI>()) se
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(FULL, cnt, off);
         fail_now = cnt < K;
+        ring_cnt = cnt;
       }
 
       // Producer of run lists: the rows of the ring in groups of 32, each
@@ -590,7 +597,11 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D, DI>()) se
             uint32_t cnt = re - rs;
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(FULL, cnt, off);
-            if (cnt < K) break;  // the whole ring holds fewer than K points
+            if (cnt < K) {  // the whole ring holds fewer than K points
+              ring_cnt = cnt;
+              fail_now = true;
+              break;
+            }
           }
           skey = ((unsigned long long)__float_as_uint(rlb) << 32) | (unsigned long long)(uint32_t)lane;
           if (sorted_rows) skey = warp_sort32(skey, lane);
@@ -711,10 +722,24 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D, DI>()) se
         const uint32_t slot = atomicAdd(p.fail_count, 1u);
         s_fail[slot] = qid;
         if (p.qradius) {
-          // the plain BETA schedule from the learned start: grow by eps0/2
-          const T rn = (T)((double)r + p.step);
-          p.qradius[qid] = rn;
-          atomicMax(p.rmax_bits, (unsigned long long)Num<T>::bits(rn));
+          // Per-query radii grow by at least eps0/2 (the plain schedule's
+          // step).  With guided growth the points found -- within the radius
+          // after a scan, or in the whole ring when it failed its count --
+          // give the local density, and the radius is scaled toward K points:
+          // (K / found)^(1/indexed dims), at most 4x per pass.  Any radius is
+          // exact; this only saves passes.
+          double rn = (double)r + p.step;
+          if (KNNSJ_GUIDED_GROWTH) {
+            const uint32_t found = fail_now ? ring_cnt : st.len;
+            const float f = exp2f(log2f((float)K / (float)max(found, 1u)) / (float)di) * 1.05f;
+            rn = fmax(rn, (double)r * (double)fminf(fmaxf(f, 1.0f), 4.0f));
+          }
+          const T rt = (T)rn;
+          p.qradius[qid] = rt;
+          atomicMax(&p.fail_radii->rmax_bits, (unsigned long long)Num<T>::bits(rt));
+          const float oct = log2f((float)rt / (2.0f * (float)p.step));  // log2(r / eps0)
+          const int bin = min(max((int)floorf(4.0f * oct) + 16, 0), FAIL_RADIUS_BINS - 1);
+          atomicAdd(&p.fail_radii->hist[bin], 1u);
         }
       }
       __syncwarp();
@@ -792,7 +817,7 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s) {
   p.fail_count = a.fail_count;
   p.cand_count = a.cand_count;
   p.work_counter = a.work_counter;
-  p.rmax_bits = a.rmax_bits;
+  p.fail_radii = a.fail_radii;
   KNNSJ_CUDA(cudaMemsetAsync(a.work_counter, 0, sizeof(uint32_t), s));
   const bool full = a.grid.geom.di == a.d;  // every dimension indexed
   switch (a.d) {

@@ -141,13 +141,24 @@ struct LoopCtl {
   double step;         // radius growth per pass
   double rmax;         // largest radius the next pass searches
   double rmax_seen;    // largest radius of any pass
-  double r_limit;      // a grid rebuild is due when rmax > r_limit and rmax > width
+  double rgrid;        // radius the grid must suit (plain: r; per-query: median failing radius)
+  double r_limit;      // a grid rebuild is due when rgrid > r_limit and rgrid > width
   double width;
   unsigned long long queries_run;
   unsigned long long accepted;
   int per_query;       // per-query radii (learned starting radius)
   int pad;
+  double redge[64];    // upper radius of each bin of the failing-radius histogram
 };
+
+// Grown radii of the queries that failed a pass (per-query radius mode):
+// their largest value and a histogram in quarter octaves of eps0, bin
+// floor(4 log2(r / eps0)) + 16 clamped to [0, 63].
+struct FailRadii {
+  unsigned long long rmax_bits;
+  uint32_t hist[64];
+};
+constexpr int FAIL_RADIUS_BINS = 64;
 
 // Launch shape of the search kernel; 0 = the default.
 struct SearchShape {
@@ -173,7 +184,7 @@ struct SearchLaunch {
   uint32_t* fail_count = nullptr;
   unsigned long long* cand_count = nullptr;
   uint32_t* work_counter = nullptr;
-  unsigned long long* rmax_bits = nullptr;  // largest grown radius of a failure (per-query radii)
+  FailRadii* fail_radii = nullptr;          // grown radii of the failures (per-query radii)
   SearchShape shape;                        // launch shape (autotuned for batched joins)
   const LoopCtl* ctl = nullptr;             // non-null: nq, lists and radius come from here (graph passes)
 };
