@@ -150,6 +150,24 @@ def join(data: np.ndarray, k: int, di: int = 0, beta: float = 0.05, reorder: boo
     return rc, ids, dists, st
 
 
+def range_query(data_summation_order: np.ndarray, eps: float, queries, maxper: int = 4096, nthreads: int = 0):
+    """Every point within eps of each query by the reference's rule
+    (evalPoint, kernel.cu:116-161), in ascending (acc, id) order.  Returns
+    (counts, ids, dists) with rows padded to maxper."""
+    x = np.ascontiguousarray(data_summation_order)
+    n, d = x.shape
+    q = np.ascontiguousarray(queries, dtype=np.uint32)
+    counts = np.zeros(q.size, np.uint32)
+    ids = np.full((q.size, maxper), -1, np.int32)
+    dists = np.zeros((q.size, maxper), x.dtype)
+    f = getattr(lib(), "orc_range_" + _sfx(x.dtype))
+    epsc = ctypes.c_float(eps) if x.dtype == np.float32 else ctypes.c_double(eps)
+    rc = f(_ptr(x), ctypes.c_uint64(n), ctypes.c_uint32(d), epsc, _ptr(q), ctypes.c_uint64(q.size),
+           ctypes.c_uint32(maxper), _ptr(counts), _ptr(ids), _ptr(dists), ctypes.c_int(nthreads))
+    assert rc == 0, "more than maxper points within eps"
+    return counts, ids, dists
+
+
 def bruteforce(data_summation_order: np.ndarray, K: int, queries, nthreads: int = 0):
     """First K points by (acc, id) for each query, over all points."""
     x = np.ascontiguousarray(data_summation_order)
@@ -162,3 +180,65 @@ def bruteforce(data_summation_order: np.ndarray, K: int, queries, nthreads: int 
            ctypes.c_uint64(q.size), _ptr(ids), _ptr(dists), ctypes.c_int(nthreads))
     assert rc == 0
     return ids, dists
+
+
+_RK_PATH = os.path.join(_HERE, "_build", "libref_kernel_runner.so")
+REF_DIR = os.path.join(_HERE, "_ref")
+
+
+def ref_kernel_cubin(dtype, d: int, di: int) -> str:
+    """Path of the reference kernel built by build_ref_kernel.sh for (DTYPE, GPUNUMDIM, NUMINDEXEDDIM)."""
+    name = "float" if np.dtype(dtype) == np.float32 else "double"
+    return os.path.join(REF_DIR, f"refkernel_{name}_{d}_{di}.cubin")
+
+
+def ref_kernel_pairs(x_reordered: np.ndarray, di: int, eps: float, queries=None, threads_per_point: int = 8):
+    """Runs the reference's own kernelNDGridIndexGlobalkNN (kernel.cu:61-113)
+    once at radius eps on the GPU, over the grid index the oracle builds
+    (pinned against the reference's host code).  Returns every (query,
+    point, distance) the kernel found within eps, unsorted."""
+    x = np.ascontiguousarray(x_reordered)
+    n, d = x.shape
+    cubin = ref_kernel_cubin(x.dtype, d, di)
+    if not os.path.exists(cubin):
+        raise FileNotFoundError(cubin)
+    if not os.path.exists(_RK_PATH):
+        build(force=True)
+    g = grid(x, di, eps)
+    q = np.arange(n, dtype=np.uint32) if queries is None else np.ascontiguousarray(queries, dtype=np.uint32)
+    # capacity: the points of the 3^di cells the kernel visits around each
+    # query's cell -- its cell coordinate computed in the data type exactly as
+    # the kernel does (kernel.cu:93) -- doubled plus a margin, so that the
+    # kernel's unchecked appends (kernel.cu:149-153) cannot overflow
+    T = x.dtype.type
+    cells = np.floor((x[:, :di] - g["minArr"]) / T(eps)).astype(np.int64)
+    mult = np.cumprod(np.concatenate([[1], g["nCells"][:-1].astype(np.int64)]))
+    counts = (g["indexmax"] - g["indexmin"] + 1).astype(np.int64)
+    keys = g["cellKeys"].astype(np.int64)
+    cap = 0
+    import itertools
+    for off in itertools.product(range(-1, 2), repeat=di):
+        c = cells[q] + np.array(off)
+        ok = np.all((c >= 0) & (c < g["nCells"].astype(np.int64)), axis=1)
+        lin = (c * mult).sum(axis=1)
+        pos = np.searchsorted(keys, lin)
+        pos = np.minimum(pos, keys.size - 1)
+        hit = ok & (keys[pos] == lin)
+        cap += int(counts[pos][hit].sum())
+    cap = 2 * cap + 1_000_000
+    out_q = np.empty(cap, np.int32)
+    out_p = np.empty(cap, np.int32)
+    out_d = np.empty(cap, x.dtype)
+    cnt = ctypes.c_uint64(0)
+    err = ctypes.create_string_buffer(512)
+    rk = ctypes.CDLL(_RK_PATH)
+    epsv = np.array([eps], x.dtype)
+    rc = rk.refk_run(cubin.encode(), ctypes.c_int(x.dtype.itemsize), _ptr(x), ctypes.c_uint64(n), ctypes.c_uint32(d),
+                     _ptr(epsv), _ptr(g["minArr"]), _ptr(g["nCells"]), ctypes.c_uint32(di), _ptr(g["cellKeys"]),
+                     _ptr(g["indexmin"]), _ptr(g["indexmax"]), ctypes.c_uint64(g["cellKeys"].size), _ptr(g["lookup"]),
+                     _ptr(q), ctypes.c_uint32(q.size), ctypes.c_uint32(threads_per_point), ctypes.c_uint64(cap),
+                     _ptr(out_q), _ptr(out_p), _ptr(out_d), ctypes.byref(cnt), err, ctypes.c_int(512))
+    if rc != 0:
+        raise RuntimeError("reference kernel: " + err.value.decode())
+    m = cnt.value
+    return out_q[:m].copy(), out_p[:m].copy(), out_d[:m].copy()

@@ -13,7 +13,12 @@
 // tests/golden/make_golden.py through oracle/build_ref_host.sh).  The
 // epsilon estimator and the range search live in the reference only as CUDA
 // kernels; their restatement below follows kernel.cu / GPU.cu line by line
-// and is cross-checked against an independent brute-force definition.
+// and is cross-checked against an independent brute-force definition.  The
+// range search's arithmetic is also pinned on the GPU against the reference
+// kernel itself: tests/test_reference_kernel.py runs kernelNDGridIndexGlobalkNN
+// (compiled from the reference's kernel.cu by build_ref_kernel.sh, launched
+// by ref_kernel_runner.cpp) and requires its within-epsilon pairs to equal
+// orc_range_* bit for bit.
 //
 // Arithmetic conventions (shared with the CUDA path):
 //   * squared distance: acc = fma(p_l - q_l, p_l - q_l, acc) for l = 0..d-1
@@ -628,6 +633,43 @@ int bruteforce_impl(const T* data, uint64_t n, uint32_t d, uint32_t K, const uin
   return 0;
 }
 
+// Brute-force range query with the reference's within-epsilon rule
+// (evalPoint, kernel.cu:116-161: acc <= fl(eps*eps) on the way, then
+// sqrt(acc) <= eps): for each listed query, every point within eps in
+// ascending (acc, id) order, at most maxper of them (counts are exact).
+template <typename T>
+int range_impl(const T* data, uint64_t n, uint32_t d, T eps, const uint32_t* queries, uint64_t nq,
+               uint32_t maxper, uint32_t* counts, int32_t* out_ids, T* out_dists, int nthreads) {
+  if (!data || !queries || !counts) return 1;
+  nthreads = clamp_threads(nthreads);
+  const T eps2 = eps * eps;
+  int bad = 0;
+#pragma omp parallel num_threads(nthreads)
+  {
+    std::vector<Cand<T>> c;
+#pragma omp for schedule(dynamic, 4) reduction(| : bad)
+    for (int64_t a = 0; a < (int64_t)nq; a++) {
+      const uint32_t q = queries[a];
+      c.clear();
+      for (uint64_t p = 0; p < n; p++) {
+        const T acc = sqdist(data + p * d, data + (uint64_t)q * d, d);
+        if (acc <= eps2 && std::sqrt(acc) <= eps) c.push_back({acc, (uint32_t)p});
+      }
+      std::sort(c.begin(), c.end());
+      counts[a] = (uint32_t)c.size();
+      if (c.size() > maxper) {
+        bad = 1;
+        continue;
+      }
+      for (size_t i = 0; i < c.size(); i++) {
+        out_ids[a * maxper + i] = (int32_t)c[i].id;
+        out_dists[a * maxper + i] = std::sqrt(c[i].acc);
+      }
+    }
+  }
+  return bad ? 2 : 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -658,6 +700,12 @@ extern "C" {
     return join_impl<T>(data, n, d, k, di, beta, reorder, queries, nq, max_iterations,       \
                         out_ids, out_dists, st ? st : &local, nthreads);                     \
   }                                                                                          \
+  int orc_range_##SUFFIX(const T* data, uint64_t n, uint32_t d, T eps, const uint32_t* queries, \
+                         uint64_t nq, uint32_t maxper, uint32_t* counts, int32_t* out_ids,          \
+                         T* out_dists, int nthreads) {                                              \
+    return range_impl<T>(data, n, d, eps, queries, nq, maxper, counts, out_ids, out_dists,        \
+                         nthreads);                                                                 \
+  }                                                                                                 \
   int orc_bruteforce_##SUFFIX(const T* data, uint64_t n, uint32_t d, uint32_t K,             \
                               const uint32_t* queries, uint64_t nq, int32_t* out_ids,        \
                               T* out_dists, int nthreads) {                                  \
