@@ -242,3 +242,30 @@ def ref_kernel_pairs(x_reordered: np.ndarray, di: int, eps: float, queries=None,
         raise RuntimeError("reference kernel: " + err.value.decode())
     m = cnt.value
     return out_q[:m].copy(), out_p[:m].copy(), out_d[:m].copy()
+
+
+def ref_eps_kernels(x_reordered: np.ndarray, di: int, k: int, beta: float):
+    """Runs the reference's epsilon-estimator kernels (kernel.cu:343-381 and
+    450-523) on the GPU with their launch shapes (GPU.cu:3275, 3434); the
+    histogram kernel gets the oracle's mean and bucket width.  Returns
+    (oracle estimate, reference histogram[10001], reference distance total,
+    reference pair count)."""
+    x = np.ascontiguousarray(x_reordered)
+    n, d = x.shape
+    cubin = ref_kernel_cubin(x.dtype, d, di)
+    if not os.path.exists(cubin):
+        raise FileNotFoundError(cubin)
+    if not os.path.exists(_RK_PATH):
+        build(force=True)
+    est = estimate_eps(x, k, beta)
+    hist = np.zeros(10001, np.uint32)
+    total = ctypes.c_double(0.0)
+    cnt = ctypes.c_ulonglong(0)
+    err = ctypes.create_string_buffer(512)
+    rk = ctypes.CDLL(_RK_PATH)
+    rc = rk.refk_eps(cubin.encode(), ctypes.c_int(x.dtype.itemsize), _ptr(x), ctypes.c_uint64(n), ctypes.c_uint32(d),
+                     ctypes.c_double(est["avg"]), ctypes.c_double(est["bucket_width"]), ctypes.c_uint32(est["offset"]),
+                     _ptr(hist), ctypes.byref(total), ctypes.byref(cnt), err, ctypes.c_int(512))
+    if rc != 0:
+        raise RuntimeError("reference eps kernels: " + err.value.decode())
+    return est, hist, total.value, cnt.value

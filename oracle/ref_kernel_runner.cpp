@@ -1,4 +1,5 @@
-// ref_kernel_runner.cpp -- runs the reference's own range-search kernel.
+// ref_kernel_runner.cpp -- runs the reference's own range-search and
+// epsilon-estimator kernels.
 //
 // TEST INFRASTRUCTURE ONLY.  Loads a cubin made by build_ref_kernel.sh from
 // the reference's kernel.cu (kernelNDGridIndexGlobalkNN, kernel.cu:61-113,
@@ -16,6 +17,7 @@
 // code of the reference.
 #include <cuda.h>
 
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -56,6 +58,8 @@ struct DevMem {
   }
 };
 
+CUfunction find_kernel(Ctx& c, CUmodule mod, const char* want);
+
 bool upload(Ctx& c, DevMem& m, const void* src, size_t bytes) {
   RK(cuMemAlloc(&m.p, bytes < 16 ? 16 : bytes));
   if (src && bytes) RK(cuMemcpyHtoD(m.p, src, bytes));
@@ -74,20 +78,8 @@ bool run(Ctx& c, const char* cubin, int tbytes, const void* data, uint64_t n, ui
   RK(cuCtxSetCurrent(ctx));
   CUmodule mod;
   RK(cuModuleLoad(&mod, cubin));
-  unsigned int nf = 0;
-  RK(cuModuleGetFunctionCount(&nf, mod));
-  std::vector<CUfunction> fs(nf);
-  RK(cuModuleEnumerateFunctions(fs.data(), nf, mod));
-  CUfunction kern = nullptr;
-  for (CUfunction f : fs) {
-    const char* name = nullptr;
-    RK(cuFuncGetName(&name, f));
-    if (name && std::strstr(name, "kernelNDGridIndexGlobalkNN")) kern = f;
-  }
-  if (!kern) {
-    std::snprintf(c.err, c.errlen, "kernelNDGridIndexGlobalkNN not in %s", cubin);
-    return false;
-  }
+  CUfunction kern = find_kernel(c, mod, "kernelNDGridIndexGlobalkNN");
+  if (!kern) return false;
   std::vector<GridCell> grid(nne);
   std::vector<GridCellLookup> gcl(nne);
   for (uint64_t i = 0; i < nne; i++) {
@@ -132,7 +124,81 @@ bool run(Ctx& c, const char* cubin, int tbytes, const void* data, uint64_t n, ui
   return true;
 }
 
+CUfunction find_kernel(Ctx& c, CUmodule mod, const char* want) {
+  unsigned int nf = 0;
+  if (cuModuleGetFunctionCount(&nf, mod) != CUDA_SUCCESS) return nullptr;
+  std::vector<CUfunction> fs(nf);
+  if (cuModuleEnumerateFunctions(fs.data(), nf, mod) != CUDA_SUCCESS) return nullptr;
+  for (CUfunction f : fs) {
+    const char* name = nullptr;
+    if (cuFuncGetName(&name, f) == CUDA_SUCCESS && name && std::strstr(name, want)) return f;
+  }
+  std::snprintf(c.err, c.errlen, "%s not in the cubin", want);
+  return nullptr;
+}
+
+// The epsilon estimator's two kernels (kernel.cu:343-381, 450-523) with the
+// reference's launch shapes (GPU.cu:3275-3290, 3440-3456): the sampled mean
+// distance (an unordered double atomic sum, so only its count is exact) and
+// the 10 000-bucket histogram, the latter run with the caller's mean and
+// bucket width so that its integer counts can be compared exactly.
+bool run_eps(Ctx& c, const char* cubin, int tbytes, const void* data, uint64_t n, uint32_t d, double avg_in,
+             double bucket_width, uint32_t offset, uint32_t* hist_out, double* total_out,
+             unsigned long long* cnt_out) {
+  RK(cuInit(0));
+  CUdevice dev;
+  RK(cuDeviceGet(&dev, 0));
+  CUcontext ctx;
+  RK(cuDevicePrimaryCtxRetain(&ctx, dev));
+  RK(cuCtxSetCurrent(ctx));
+  CUmodule mod;
+  RK(cuModuleLoad(&mod, cubin));
+  CUfunction kavg = find_kernel(c, mod, "kernelEstimateAvgDistBruteForce");
+  CUfunction khist = find_kernel(c, mod, "kernelKDistBruteForce");
+  if (!kavg || !khist) return false;
+  const unsigned int N = (unsigned int)n, zero = 0, off = offset;
+  const unsigned long long zero64 = 0;
+  const double dz = 0.0;
+  // one spare bucket: a distance just below the mean can round to bucket
+  // 10000, which the reference writes without a check (kernel.cu:511-512)
+  std::vector<uint32_t> hz(10001, 0);
+  DevMem dN, dbg1, dbg2, dcnt, ddata, dtot, doff, dcnt2, davg, dhist, dbw;
+  bool ok = upload(c, dN, &N, 4) && upload(c, dbg1, &zero, 4) && upload(c, dbg2, &zero, 4) &&
+            upload(c, dcnt, &zero64, 8) && upload(c, ddata, data, n * d * tbytes) && upload(c, dtot, &dz, 8) &&
+            upload(c, doff, &off, 4) && upload(c, dcnt2, &zero64, 8) && upload(c, davg, &avg_in, 8) &&
+            upload(c, dhist, hz.data(), hz.size() * 4) && upload(c, dbw, &bucket_width, 8);
+  if (!ok) return false;
+  const unsigned int block = 256;
+  // GPU.cu:3275: TOTALBLOCKS = ceil((0.001*N)/(1.0*BLOCKSIZE))
+  const unsigned int blocks_avg = (unsigned int)std::ceil((0.001 * N) / (1.0 * block));
+  void* a_avg[] = {&dN.p, &dbg1.p, &dbg2.p, &dcnt.p, &ddata.p, &dtot.p};
+  RK(cuLaunchKernel(kavg, blocks_avg, 1, 1, block, 1, 1, 0, nullptr, a_avg, nullptr));
+  const unsigned int blocks_hist = N / offset;  // GPU.cu:3434: ceil((*N)/(*offset)) of an integer quotient
+  void* a_hist[] = {&dN.p, &doff.p, &dbg1.p, &dbg2.p, &dcnt2.p, &ddata.p, &davg.p, &dhist.p, &dbw.p};
+  if (blocks_hist > 0) RK(cuLaunchKernel(khist, blocks_hist, 1, 1, block, 1, 1, 0, nullptr, a_hist, nullptr));
+  RK(cuCtxSynchronize());
+  RK(cuMemcpyDtoH(total_out, dtot.p, 8));
+  RK(cuMemcpyDtoH(cnt_out, dcnt.p, 8));
+  RK(cuMemcpyDtoH(hist_out, dhist.p, 10001 * 4));
+  RK(cuModuleUnload(mod));
+  return true;
+}
+
 }  // namespace
+
+extern "C" int refk_eps(const char* cubin, int tbytes, const void* data, uint64_t n, uint32_t d, double avg_in,
+                        double bucket_width, uint32_t offset, uint32_t* hist_out /*10001*/, double* total_out,
+                        unsigned long long* cnt_out, char* err, int errlen) {
+  Ctx c{err, errlen};
+  if (err && errlen > 0) err[0] = 0;
+  if (n % 256 != 0 || offset == 0) {
+    // the histogram kernel reads up to 255 points past the last stride
+    // (kernel.cu:486-492); a multiple of 256 points keeps every read in range
+    std::snprintf(err, errlen, "n must be a multiple of 256 and offset positive");
+    return 1;
+  }
+  return run_eps(c, cubin, tbytes, data, n, d, avg_in, bucket_width, offset, hist_out, total_out, cnt_out) ? 0 : 1;
+}
 
 extern "C" int refk_run(const char* cubin, int tbytes, const void* data, uint64_t n, uint32_t d, const void* eps,
                         const void* minArr, const uint32_t* nCells, uint32_t di, const uint64_t* cellKeys,

@@ -58,3 +58,23 @@ def test_reference_kernel_pairs_equal_oracle_range(case):
     assert np.array_equal(ref_ids, orc_ids)
     ub = np.uint32 if np_dtype == np.float32 else np.uint64
     assert np.array_equal(ref_d.view(ub), orc_d.view(ub))
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}_{c[1]}_{c[2]}")
+def test_reference_eps_kernels_equal_oracle(case):
+    # the histogram's integer counts exactly (same mean and bucket width
+    # given); the mean's pair count exactly and its double sum to rounding
+    # (the reference adds it with atomics in no fixed order)
+    dtype, d, di, n, k, beta, gen = case
+    np_dtype = np.float32 if dtype == "float" else np.float64
+    if not os.path.exists(oracle.ref_kernel_cubin(np_dtype, d, di)):
+        pytest.skip("reference kernel cubin not built (the reference sources were absent when build() ran)")
+    n = (n // 256) * 256  # whole 256-point strides: the histogram kernel reads no point past N
+    x = np.ascontiguousarray(gen(n), dtype=np_dtype)
+    perm, _ = oracle.reorder(x)
+    xr = np.ascontiguousarray(x[:, perm])
+    est, hist, total, cnt = oracle.ref_eps_kernels(xr, di, k, beta)
+    assert cnt == est["pair_count"]
+    assert abs(total / cnt - est["avg"]) <= 1e-12 * est["avg"]
+    assert np.array_equal(hist[:10000], est["hist"])
+    assert hist[:10000].sum() > 0
