@@ -43,6 +43,9 @@ namespace {
 
 constexpr int SEARCH_THREADS = 256;  // largest block; the launch may use fewer warps
 constexpr int QCHUNK = 4;            // default queries per work fetch
+#ifndef KNNSJ_QCHUNK_PER_QUERY_RADIUS
+#define KNNSJ_QCHUNK_PER_QUERY_RADIUS 1
+#endif
 // ring rows per wave (each row is one run of points): for one or two indexed
 // dimensions, and for more (wider rings of shorter rows)
 #ifndef KNNSJ_WAVE_ROWS_LO
@@ -260,8 +263,16 @@ __device__ void hist_reduce(typename Key<T>::type* buf, uint32_t* hist, Sel<T>& 
 
 // Rare paths are kept out of line so the hot loop stays small in the
 // instruction cache.
+#ifndef KNNSJ_REDUCE_CALLED
+#define KNNSJ_REDUCE_CALLED 1
+#endif
+#if KNNSJ_REDUCE_CALLED
+#define KNNSJ_REDUCE_LINKAGE __noinline__
+#else
+#define KNNSJ_REDUCE_LINKAGE __forceinline__
+#endif
 template <typename T>
-__device__ __noinline__ Sel<T> reduce(typename Key<T>::type* buf, uint32_t* hist, Sel<T> st, uint32_t K, uint32_t B,
+__device__ KNNSJ_REDUCE_LINKAGE Sel<T> reduce(typename Key<T>::type* buf, uint32_t* hist, Sel<T> st, uint32_t K, uint32_t B,
                                       int lane) {
   if (B <= HIST_MAX_B)
     hist_reduce<T>(buf, hist, st, K, B, lane);
@@ -270,11 +281,21 @@ __device__ __noinline__ Sel<T> reduce(typename Key<T>::type* buf, uint32_t* hist
   return st;
 }
 
+// the output sort is inlined (0: measured faster) or a called function (1)
+#ifndef KNNSJ_WRITE_CALLED
+#define KNNSJ_WRITE_CALLED 0
+#endif
+#if KNNSJ_WRITE_CALLED
+#define KNNSJ_WRITE_LINKAGE __noinline__
+#else
+#define KNNSJ_WRITE_LINKAGE __forceinline__
+#endif
+
 // Writes the K smallest of buf[0..len) in ascending (distance, id) order by a
 // counting sort over 256 bins of a monotone map of the distance (all keys are
 // <= acc(top)), ranking keys that share a bin among themselves.  len <= 256.
 template <typename T>
-__device__ __noinline__ void write_sorted_row(typename Key<T>::type* buf, uint32_t* cnt, uint32_t len,
+__device__ KNNSJ_WRITE_LINKAGE void write_sorted_row(typename Key<T>::type* buf, uint32_t* cnt, uint32_t len,
                                               typename Key<T>::type top, uint32_t K, int32_t* __restrict__ out_ids,
                                               T* __restrict__ out_d, uint64_t row_out, int lane) {
   using Kt = Key<T>;
@@ -391,22 +412,22 @@ __device__ __forceinline__ unsigned long long warp_sort32(unsigned long long v, 
   return v;
 }
 
-// resident blocks per SM the register budget is cut for: low dimensions
-// (d <= 3, all indexed) fit 64 registers, higher ones need more
+// resident blocks per SM the register budget is cut for: float data in low
+// dimensions (d <= 3, all indexed) fits 64 registers, the rest needs more
 #ifndef KNNSJ_MINB_LO
 #define KNNSJ_MINB_LO 4
 #endif
 #ifndef KNNSJ_MINB_HI
 #define KNNSJ_MINB_HI 3
 #endif
-template <int D, int DI>
+template <typename T, int D, int DI>
 constexpr int search_min_blocks() {
-  return (D > 0 && D <= 3 && DI > 0) ? KNNSJ_MINB_LO : KNNSJ_MINB_HI;
+  return (sizeof(T) == 4 && D > 0 && D <= 3 && DI > 0) ? KNNSJ_MINB_LO : KNNSJ_MINB_HI;
 }
 
 // D: data dimensions (0 = runtime); DI: indexed dimensions (0 = runtime, <= MAX_DI).
 template <typename T, int D, int DI>
-__global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<D, DI>()) search_kernel(const SearchParams<T> p) {
+__global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>()) search_kernel(const SearchParams<T> p) {
   constexpr int WAVE_ROWS = wave_rows<DI>();
   constexpr int NDI = DI > 0 ? DI : MAX_DI;
   using Kt = Key<T>;
@@ -803,7 +824,9 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s) {
   if (a.shape.buffer > 0 && (uint32_t)a.shape.buffer > p.B && (a.shape.buffer & (a.shape.buffer - 1)) == 0 &&
       a.shape.buffer <= 4096)
     p.B = (uint32_t)a.shape.buffer;
-  p.qchunk = a.shape.qchunk > 0 ? (uint32_t)a.shape.qchunk : (uint32_t)QCHUNK;
+  // per-query radii make the work per query uneven: finer work fetching
+  p.qchunk = a.shape.qchunk > 0 ? (uint32_t)a.shape.qchunk
+                                : (uint32_t)(a.qradius ? KNNSJ_QCHUNK_PER_QUERY_RADIUS : QCHUNK);
   const int wpb = a.shape.warps_per_block;
   p.qlist = a.qlist;
   p.nq = a.nq;
