@@ -26,6 +26,7 @@
 // are computed exactly as the reference does.  The bucket is always the
 // reference's double-precision bucket.
 
+#include "exact_sqrt.cuh"
 #include "knnsj_internal.h"
 
 namespace knnsj {
@@ -46,6 +47,17 @@ __device__ __forceinline__ double eps_term(double acc, float a, float b) {
 __device__ __forceinline__ double eps_term(double acc, double a, double b) {
   const double df = __dsub_rn(a, b);
   return __fma_rn(df, df, acc);
+}
+
+// The first term of the sum, which the reference adds to 0.0: the same value
+// without the FP64 addition.
+__device__ __forceinline__ double eps_first(float a, float b) {
+  const float df = __fsub_rn(a, b);
+  return (double)__fmul_rn(df, df);
+}
+__device__ __forceinline__ double eps_first(double a, double b) {
+  const double df = __dsub_rn(a, b);
+  return __dmul_rn(df, df);
 }
 
 __host__ __device__ __forceinline__ uint64_t terms_of_sample(uint64_t g, uint64_t n) {
@@ -70,17 +82,21 @@ __global__ void eps_avg_chunk_kernel(const T* __restrict__ soa, uint64_t n, uint
     constexpr int U = 4;
     for (uint64_t m = (uint64_t)c * EPS_CHUNK; m < m_end; m += U) {
       double rd[U];
+      {
+        const T q0 = soa[tid];
 #pragma unroll
-      for (int u = 0; u < U; u++) rd[u] = 0.0;
-      for (uint32_t l = 0; l < d; l++) {
+        for (int u = 0; u < U; u++) rd[u] = m + u < m_end ? eps_first(soa[t + 1000 * (m + u)], q0) : 0.0;
+      }
+      for (uint32_t l = 1; l < d; l++) {
         const T ql = soa[(uint64_t)l * n + tid];
 #pragma unroll
         for (int u = 0; u < U; u++)
           if (m + u < m_end) rd[u] = eps_term(rd[u], soa[(uint64_t)l * n + t + 1000 * (m + u)], ql);
       }
+      // the correctly rounded double root, computed on the integer pipes
 #pragma unroll
       for (int u = 0; u < U; u++)
-        if (m + u < m_end) s = __dadd_rn(s, __dsqrt_rn(rd[u]));
+        if (m + u < m_end) s = __dadd_rn(s, exact_sqrt(rd[u]));
     }
   }
   partial[w] = s;
