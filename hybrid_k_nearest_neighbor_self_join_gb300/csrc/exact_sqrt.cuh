@@ -76,12 +76,64 @@ __host__ __device__ inline U128 es_rem(U128 M, uint64_t y) {
   return r;
 }
 
-// A float close to the signed 128-bit value r (|r| < 2^100).
+// Conversions between 64-bit integers and floats run on the FP64 pipe on this
+// GPU, which is what this file avoids: floats are assembled from and taken
+// apart into bits with integer operations (truncating; Newton absorbs it).
+__host__ __device__ inline float es_float_bits(uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(b);
+#else
+  float f;
+  std::memcpy(&f, &b, 4);
+  return f;
+#endif
+}
+
+__host__ __device__ inline uint32_t es_bits_of_float(float f) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(f);
+#else
+  uint32_t b;
+  std::memcpy(&b, &f, 4);
+  return b;
+#endif
+}
+
+// A float close to (within 2^-23 of) the unsigned value v = hi:lo > 0.
+__host__ __device__ inline float es_u128_to_float(uint64_t hi, uint64_t lo) {
+  int p;  // index of the leading one
+  uint64_t top;
+  if (hi) {
+    p = 127 - es_clz64(hi);
+    top = p >= 64 + 23 ? (hi >> (p - 64 - 23)) : ((hi << (64 + 23 - p)) | (lo >> (p - 23)));
+  } else {
+    p = 63 - es_clz64(lo);
+    top = p >= 23 ? (lo >> (p - 23)) : (lo << (23 - p));
+  }
+  return es_float_bits((uint32_t)((p + 127) << 23) | (uint32_t)(top & 0x7fffffu));
+}
+
+// A float close to the signed 128-bit value r.
 __host__ __device__ inline float es_to_float(U128 r) {
-  if ((int64_t)r.hi == ((int64_t)r.lo >> 63)) return (float)(int64_t)r.lo;  // fits in 64 bits
-  // r >> 40 (arithmetic) fits in 64 bits for |r| < 2^103
-  const int64_t top = (int64_t)((r.hi << 24) | (r.lo >> 40));
-  return (float)top * 1099511627776.0f;  // * 2^40
+  const bool neg = (int64_t)r.hi < 0;
+  uint64_t lo = r.lo, hi = r.hi;
+  if (neg) {  // two's complement negate
+    lo = ~lo + 1;
+    hi = ~hi + (lo == 0 ? 1 : 0);
+  }
+  if (!hi && !lo) return 0.0f;
+  const float f = es_u128_to_float(hi, lo);
+  return neg ? -f : f;
+}
+
+// The integer nearest below |f| (truncation toward zero), with f's sign.
+__host__ __device__ inline int64_t es_float_to_i64(float f) {
+  const uint32_t b = es_bits_of_float(f);
+  const int e = (int)((b >> 23) & 0xff) - 127;
+  if (e < 0) return 0;
+  const uint64_t mant = (uint64_t)((b & 0x7fffffu) | 0x800000u);
+  const uint64_t v = e >= 23 ? mant << (e - 23) : mant >> (23 - e);
+  return (b >> 31) ? -(int64_t)v : (int64_t)v;
 }
 
 // sqrt(x) rounded to nearest, for finite x >= 0 (any other input returns x).
@@ -103,13 +155,14 @@ __host__ __device__ inline double exact_sqrt(double x) {
   U128 M;
   M.lo = m << k;
   M.hi = m >> (64 - k);
-  // float seed: sqrt(m * 2^(k-52)) * 2^26
-  const float mf = (float)(m << (k - 52));
-  uint64_t y = (uint64_t)(sqrtf(mf) * 67108864.0f);
+  // float seed: sqrt(m * 2^(k-52)) * 2^26, m truncated to 24 bits
+  const float mf = es_float_bits((uint32_t)((127 + k) << 23) | (uint32_t)((m >> 29) & 0x7fffffu));
+  const uint32_t sb = es_bits_of_float(sqrtf(mf));  // in [2^26, 2^27)
+  uint64_t y = (uint64_t)((sb & 0x7fffffu) | 0x800000u) << ((int)((sb >> 23) & 0xff) - 127 + 3);
   for (int it = 0; it < 2; it++) {
     const U128 r = es_rem(M, y);
-    const float d = es_to_float(r) / (2.0f * (float)y);
-    y = (uint64_t)((int64_t)y + (int64_t)d);
+    const float d = es_to_float(r) / (2.0f * es_u128_to_float(0, y));
+    y = (uint64_t)((int64_t)y + es_float_to_i64(d));
   }
   // final correction: 0 <= r <= 2y
   int64_t r = (int64_t)es_rem(M, y).lo;  // |r| < 2^63 here
