@@ -604,9 +604,14 @@ knnsj_status knnsj_radius_predict(const float* model, const float* features, uin
         float* dy = (float*)w.dists.get(std::max<uint64_t>(n, 1) * 4);
         KNNSJ_CUDA(cudaMemcpyAsync(dm, model, KNNSJ_RADIUS_MODEL_FLOATS * 4, cudaMemcpyHostToDevice, s));
         KNNSJ_CUDA(cudaMemcpyAsync(df, features, n * KNNSJ_RADIUS_FEATURES * 4, cudaMemcpyHostToDevice, s));
-        launch_mlp_predict(dm, df, n, dy, s);
+        uint32_t* derr = (uint32_t*)w.flags.get(4);
+        KNNSJ_CUDA(cudaMemsetAsync(derr, 0, 4, s));
+        launch_mlp_predict(dm, df, n, dy, derr, w.sm_count, s);
+        uint32_t herr = 0;
         KNNSJ_CUDA(cudaMemcpyAsync(out, dy, n * 4, cudaMemcpyDeviceToHost, s));
+        KNNSJ_CUDA(cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, s));
         KNNSJ_CUDA(cudaStreamSynchronize(s));
+        if (herr) throw StatusError{KNNSJ_ERR_CUDA, "tensor-core radius model timed out"};
       },
       nullptr);
 }

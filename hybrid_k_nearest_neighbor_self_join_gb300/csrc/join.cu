@@ -144,6 +144,7 @@ struct SmallDev {  // layout of Workspace::small
   double cpart[1024];
   FailRadii fr;
   LoopCtl ctl;
+  uint32_t mlp_err;  // the tensor-core radius MLP timed out
 };
 
 template <typename T>
@@ -547,8 +548,9 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   double rmax = (double)P.eps0;
   if (cfg.radius_mode == KNNSJ_RADIUS_LEARNED) {
     qrad = (T*)w.qradius.get(n * sizeof(T));
+    KNNSJ_CUDA(cudaMemsetAsync(&sm->mlp_err, 0, 4, s));
     launch_radius_assign<T>(P.grid, n, d, k, (float)cfg.beta, device_model(w, s), (double)P.eps0,
-                            (float)cfg.radius_offset, qrad, s);
+                            (float)cfg.radius_offset, qrad, &sm->mlp_err, w.sm_count, s);
     rmax = (double)P.eps0 * learned_max_cells(di);
   }
 
@@ -682,8 +684,12 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   }
   rec(2);
   unsigned long long cand = 0;
+  uint32_t mlp_err = 0;
   KNNSJ_CUDA(cudaMemcpyAsync(&cand, &sm->cand, 8, cudaMemcpyDeviceToHost, s));
+  if (qrad) KNNSJ_CUDA(cudaMemcpyAsync(&mlp_err, &sm->mlp_err, 4, cudaMemcpyDeviceToHost, s));
   KNNSJ_CUDA(cudaStreamSynchronize(s));
+  if (mlp_err)  // rows are still exact: the affected queries started at eps0
+    fprintf(stderr, "knnsj: the tensor-core radius model timed out; those queries started at eps0\n");
   if (st) {
     st->iterations = iter;
     st->regrids = regrids;

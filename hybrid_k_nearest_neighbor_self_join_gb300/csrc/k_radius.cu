@@ -4,10 +4,13 @@
 // points and the same cell-table entries).  The model lives in shared memory.
 
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
 #include "knnsj_internal.h"
+#include "mlp_tc.cuh"
 #include "radius_model.cuh"
 
 namespace knnsj {
@@ -106,6 +109,69 @@ __global__ void __launch_bounds__(RA_THREADS) mlp_predict_kernel(const float* __
   out[i] = mlp_eval_blocked(sm, f);
 }
 
+// Front-ends of the tensor-core MLP (mlp_tc.cuh).
+// Radius assignment: features from the cell table, radius written by
+// original id; the fallback is the plain starting radius eps0.
+template <typename T>
+struct AssignSrc {
+  CellTable<T> t;
+  const T* ps;
+  const uint32_t* pid;
+  uint64_t n;
+  uint32_t d, k;
+  float beta, eps0f, log_lo, log_hi, offset;
+  T* qradius;
+  __device__ void features(uint64_t i, float* f) {
+    T q[MAX_DI];
+    for (uint32_t j = 0; j < t.g.di; j++) q[j] = ps[(uint64_t)j * n + i];
+    radius_features(t, q, d, k, beta, n, f);
+  }
+  __device__ void store(uint64_t i, float y) {
+    y = fminf(fmaxf(y + offset, log_lo), log_hi);
+    qradius[pid[i]] = (T)(eps0f * expf(y));
+  }
+  __device__ void fallback(uint64_t i) { qradius[pid[i]] = (T)eps0f; }
+};
+
+// Prediction from stored features (knnsj_radius_predict).
+struct PredictSrc {
+  const float* feat;
+  float* out;
+  __device__ void features(uint64_t i, float* f) {
+    for (int j = 0; j < NFEAT; j++) f[j] = feat[i * NFEAT + j];
+  }
+  __device__ void store(uint64_t i, float y) { out[i] = y; }
+  __device__ void fallback(uint64_t i) { out[i] = __int_as_float(0x7fc00000); }
+};
+
+template <typename Src>
+__global__ void __launch_bounds__(TC_ROWS) mlp_tc_kernel(Src src, const float* __restrict__ model, uint64_t n,
+                                                          uint32_t* err) {
+  mlp_tc_tiles(src, model, n, err);
+}
+
+template <typename Src>
+void launch_mlp_tc(const Src& src, const float* model, uint64_t n, uint32_t* err, int sm_count, cudaStream_t s) {
+  if (n == 0) return;
+  // the largest shared-memory carveout, so that several CTAs share an SM
+  // (each holds 64 of the SM's 512 TMEM columns: at most 8 fit)
+  KNNSJ_CUDA(cudaFuncSetAttribute(mlp_tc_kernel<Src>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxShared));
+  // CTAs per SM by registers and shared memory (the occupancy query does not
+  // count co-resident CTAs of a kernel that allocates TMEM), at most what
+  // the SM's TMEM holds
+  cudaFuncAttributes fa;
+  KNNSJ_CUDA(cudaFuncGetAttributes(&fa, mlp_tc_kernel<Src>));
+  const int regs = std::max(fa.numRegs, 1) * TC_ROWS;
+  int per_sm = std::min(65536 / regs, (int)((227 * 1024) / std::max<size_t>(fa.sharedSizeBytes + 1024, 1)));
+  per_sm = std::max(1, std::min(per_sm, 512 / TC_TMEM_COLS));
+  const uint64_t tiles = (n + TC_ROWS - 1) / TC_ROWS;
+  uint64_t blocks = (uint64_t)std::max(per_sm, 1) * (uint64_t)std::max(sm_count, 1);
+  if (blocks > tiles) blocks = tiles;
+  mlp_tc_kernel<Src><<<(unsigned)blocks, TC_ROWS, 0, s>>>(src, model, n, err);
+  KNNSJ_CHECK_LAUNCH();
+}
+
 }  // namespace
 
 // Largest ring half-width (in cells of the eps0 grid) a learned radius may
@@ -123,11 +189,24 @@ double learned_max_cells(uint32_t di) {
   }
 }
 
+// The MLP runs on the tensor cores (BF16 operands, FP32 accumulation) unless
+// KNNSJ_RADIUS_MLP=fp32 selects the CUDA-core FP32 evaluation.
+static bool mlp_on_tensor_cores() {
+  const char* e = std::getenv("KNNSJ_RADIUS_MLP");
+  return !(e && std::strcmp(e, "fp32") == 0);
+}
+
 template <typename T>
 void launch_radius_assign(const DeviceGrid<T>& g, uint64_t n, uint32_t d, uint32_t k, float beta,
-                          const float* d_model, double eps0, float offset, T* qradius, cudaStream_t s) {
+                          const float* d_model, double eps0, float offset, T* qradius, uint32_t* d_err, int sm_count,
+                          cudaStream_t s) {
   const float log_lo = std::log(1.0f / 16.0f);
   const float log_hi = (float)std::log(learned_max_cells(g.geom.di) * (1.0 - 1.0 / 4096.0));
+  if (mlp_on_tensor_cores()) {
+    AssignSrc<T> src{table_of(g), g.ps, g.pid, n, d, k, beta, (float)eps0, log_lo, log_hi, offset, qradius};
+    launch_mlp_tc(src, d_model, n, d_err, sm_count, s);
+    return;
+  }
   radius_assign_kernel<T><<<(unsigned)((n + RA_THREADS - 1) / RA_THREADS), RA_THREADS, 0, s>>>(
       table_of(g), g.ps, g.pid, n, d, k, beta, d_model, (float)eps0, log_lo, log_hi, offset, qradius);
   KNNSJ_CHECK_LAUNCH();
@@ -141,16 +220,22 @@ void launch_radius_features(const DeviceGrid<T>& g, uint64_t n, uint32_t d, uint
   KNNSJ_CHECK_LAUNCH();
 }
 
-void launch_mlp_predict(const float* d_model, const float* d_feat, uint64_t n, float* d_out, cudaStream_t s) {
+void launch_mlp_predict(const float* d_model, const float* d_feat, uint64_t n, float* d_out, uint32_t* d_err,
+                        int sm_count, cudaStream_t s) {
   if (n == 0) return;
+  if (mlp_on_tensor_cores()) {
+    PredictSrc src{d_feat, d_out};
+    launch_mlp_tc(src, d_model, n, d_err, sm_count, s);
+    return;
+  }
   mlp_predict_kernel<<<(unsigned)((n + RA_THREADS - 1) / RA_THREADS), RA_THREADS, 0, s>>>(d_model, d_feat, n, d_out);
   KNNSJ_CHECK_LAUNCH();
 }
 
 template void launch_radius_assign<float>(const DeviceGrid<float>&, uint64_t, uint32_t, uint32_t, float,
-                                          const float*, double, float, float*, cudaStream_t);
+                                          const float*, double, float, float*, uint32_t*, int, cudaStream_t);
 template void launch_radius_assign<double>(const DeviceGrid<double>&, uint64_t, uint32_t, uint32_t, float,
-                                           const float*, double, float, double*, cudaStream_t);
+                                           const float*, double, float, double*, uint32_t*, int, cudaStream_t);
 template void launch_radius_features<float>(const DeviceGrid<float>&, uint64_t, uint32_t, uint32_t, float, float*,
                                             cudaStream_t);
 template void launch_radius_features<double>(const DeviceGrid<double>&, uint64_t, uint32_t, uint32_t, float, float*,

@@ -228,11 +228,15 @@ void run_features(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* 
 double learned_max_cells(uint32_t di);
 template <typename T>
 void launch_radius_assign(const DeviceGrid<T>& g, uint64_t n, uint32_t d, uint32_t k, float beta,
-                          const float* d_model, double eps0, float offset, T* qradius, cudaStream_t s);
+                          const float* d_model, double eps0, float offset, T* qradius, uint32_t* d_err, int sm_count,
+                          cudaStream_t s);
 template <typename T>
 void launch_radius_features(const DeviceGrid<T>& g, uint64_t n, uint32_t d, uint32_t k, float beta, float* out,
                             cudaStream_t s);
-void launch_mlp_predict(const float* d_model, const float* d_feat, uint64_t n, float* d_out, cudaStream_t s);
+// d_err is set to 1 if a tensor-core wait timed out (the outputs then hold
+// the fallback: eps0 radii, NaN predictions).
+void launch_mlp_predict(const float* d_model, const float* d_feat, uint64_t n, float* d_out, uint32_t* d_err,
+                        int sm_count, cudaStream_t s);
 // Active model: a copy and its version (changes on every set).
 unsigned radius_model_snapshot(std::vector<float>* out);
 void radius_model_set(const float* model);  // nullptr restores the built-in model

@@ -75,12 +75,48 @@ def random_model(seed):
     return m
 
 
-def test_forward_matches_numpy():
+def bf16(a):
+    """float32 -> nearest bfloat16 (ties to even), returned as float32."""
+    b = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    b = (b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000
+    return b.astype(np.uint32).view(np.float32)
+
+
+def np_forward_bf16(m, X):
+    """The tensor-core evaluation: BF16 operands (normalised features,
+    first-layer activations, W1, W2), FP32 accumulation, biases, ReLU and
+    the last layer in FP32."""
+    mean, istd = m[:NF], m[NF:2 * NF]
+    W1 = m[2 * NF:2 * NF + NF * NH].reshape(NF, NH)
+    o = 2 * NF + NF * NH
+    b1 = m[o:o + NH]; o += NH
+    W2 = m[o:o + NH * NH].reshape(NH, NH); o += NH * NH
+    b2 = m[o:o + NH]; o += NH
+    W3 = m[o:o + NH]; b3 = m[o + NH]
+    x = bf16((X - mean) * istd).astype(np.float64)
+    h1 = np.maximum(x @ bf16(W1).astype(np.float64) + b1, 0)
+    a2 = np.maximum(bf16(h1.astype(np.float32)).astype(np.float64) @ bf16(W2).astype(np.float64) + b2, 0)
+    return a2 @ W3 + b3
+
+
+def test_forward_matches_numpy(monkeypatch):
     m = random_model(1)
     X = np.random.default_rng(2).normal(0, 1, (3000, NF)).astype(np.float32)
+    # the FP32 CUDA-core evaluation: the training forward pass
+    monkeypatch.setenv("KNNSJ_RADIUS_MLP", "fp32")
     got = train_radius.predict(m, X)
     want = np_forward(m, X)[-1]
     assert np.allclose(got, want, rtol=1e-4, atol=1e-4)
+    # the tensor-core evaluation (tcgen05, BF16 operands), as the join uses
+    # it: equal to a BF16 restatement up to FP32 summation order
+    monkeypatch.delenv("KNNSJ_RADIUS_MLP")
+    got = train_radius.predict(m, X)
+    want = np_forward_bf16(m, X)
+    # (a BF16 rounding of a first-layer activation can flip with the FP32
+    # summation order: one BF16 unit, 2^-8 relative, through W2)
+    assert np.allclose(got, want, rtol=5e-3, atol=5e-2), np.abs(got - want).max()
+    assert np.corrcoef(got, want)[0, 1] > 0.9999
+    assert np.abs(got - np_forward(m, X)[-1]).max() < 0.5  # and close to the FP32 model
 
 
 @pytest.mark.parametrize("q", [0.5, 0.9])
