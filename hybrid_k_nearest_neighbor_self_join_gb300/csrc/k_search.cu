@@ -355,21 +355,36 @@ __device__ KNNSJ_WRITE_LINKAGE void write_sorted_row(typename Key<T>::type* buf,
     }
   }
   __syncwarp();
-  // rank inside the bin, then write rows below K
+  // buf is now in bin order, and the K smallest keys lie in the bins that
+  // start below K: only positions below the end of the bin holding position
+  // K-1 are ranked inside their bin and written
+  uint32_t end = 0;
+  {
+    uint32_t st = incl - s;  // start of this lane's first bin
+    uint32_t e = 0;
 #pragma unroll
-  for (int r = 0; r < R; r++) {
-    const uint32_t i = r * 32 + lane;
-    if (r * 32 < (int)len && i < len) {
-      const int b = min((int)((float)Kt::acc(v[r]) * scale), 255);
+    for (int t = 0; t < 8; t++) {
+      const uint32_t nx = st + c[t];
+      if (st < K && K <= nx) e = nx;  // bin t holds position K-1
+      st = nx;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) e = max(e, __shfl_xor_sync(FULL, e, off));
+    end = e ? e : len;
+  }
+  for (uint32_t p0 = 0; p0 < end; p0 += 32) {
+    const uint32_t pp = p0 + lane;
+    if (pp < end) {
+      const KT w = buf[pp];
+      const int b = min((int)((float)Kt::acc(w) * scale), 255);
       const uint32_t first = cnt[b];
       const uint32_t last = b < 255 ? cnt[b + 1] : len;
       uint32_t rank = 0;
-      if (first < K)
-        for (uint32_t j = first; j < last; j++) rank += Kt::less(buf[j], v[r]) ? 1u : 0u;
+      for (uint32_t j = first; j < last; j++) rank += Kt::less(buf[j], w) ? 1u : 0u;
       const uint32_t fin = first + rank;
       if (fin < K) {
-        out_ids[row_out + fin] = (int32_t)Kt::id(v[r]);
-        out_d[row_out + fin] = Num<T>::sqrt(Kt::acc(v[r]));
+        out_ids[row_out + fin] = (int32_t)Kt::id(w);
+        out_d[row_out + fin] = Num<T>::sqrt(Kt::acc(w));
       }
     }
   }
