@@ -410,6 +410,23 @@ __device__ __noinline__ void write_sorted_row_bitonic(typename Key<T>::type* buf
   __syncwarp();
 }
 
+// A lower (up = false) or upper (up = true) bound of the grid cell of
+// coordinate v, clamped to [0, ncell-1], from float arithmetic with a
+// reciprocal: (v - minf) * invw is within 2^-22 relative of (v - min) / width
+// (the rounding of v - minf, of 1/width, of the product, and of min and
+// width to float), plus 2^-24 |minf| * invw from rounding min; the bound
+// moves by twice that, so the true cell of any coordinate on the far side
+// of v (the grid's own monotone division in the data type) is never cut off.
+__device__ __forceinline__ uint32_t ring_cell(float v, float minf, float invw, uint32_t ncell, bool up) {
+  const float u = (v - minf) * invw;
+  const float tol = (fabsf(u) + fabsf(minf) * invw) * (1.0f / 2097152.0f) + (1.0f / 1048576.0f);
+  const float ub = up ? u + tol : u - tol;
+  if (!(ub > 0.0f)) return 0;
+  if (!(ub < (float)ncell)) return ncell - 1;
+  const uint32_t c = (uint32_t)ub;
+  return c < ncell ? c : ncell - 1;
+}
+
 // Bitonic sort of one 64-bit value per lane across the warp (ascending).
 __device__ __forceinline__ unsigned long long warp_sort32(unsigned long long v, int lane) {
 #pragma unroll
@@ -471,7 +488,12 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
   __shared__ const uint32_t* s_qlist;
   __shared__ uint32_t* s_fail;
   __shared__ T s_radius;
+  // the grid's origin and inverse cell width in float, for ring bounds
+  __shared__ float s_minf[NDI];
+  __shared__ float s_invw;
+  if (threadIdx.x < (unsigned)NDI) s_minf[threadIdx.x] = threadIdx.x < p.g.di ? (float)p.g.minv[threadIdx.x] : 0.0f;
   if (threadIdx.x == 0) {
+    s_invw = 1.0f / (float)p.g.width;
     if (p.ctl) {
       s_nq = p.ctl->nq;
       s_qlist = p.ctl->list[p.ctl->cur];
@@ -527,10 +549,11 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
           const T qj = qdim(j);
           qf[j] = (float)qj;
           const float slack = (fabsf(qf[j]) + rf) * (1.0f / 2097152.0f);
-          lo[j] = clamped_cell((T)(qf[j] - rf - slack), p.g.minv[j], p.g.width, p.g.ncell[j]);
-          hi[j] = clamped_cell((T)(qf[j] + rf + slack), p.g.minv[j], p.g.width, p.g.ncell[j]);
+          lo[j] = ring_cell(qf[j] - rf - slack, s_minf[j], s_invw, p.g.ncell[j], false);
+          hi[j] = ring_cell(qf[j] + rf + slack, s_minf[j], s_invw, p.g.ncell[j], true);
           const uint32_t ext = hi[j] - lo[j] + 1;
-          magic[j] = ext > 1 ? 0xffffffffu / ext + 1u : 0u;  // x / ext == umulhi(x, magic) for small x
+          // x / ext == umulhi(x, magic) for small x; rows are indexed by dims 1..
+          if (j > 0) magic[j] = ext > 1 ? 0xffffffffu / ext + 1u : 0u;
         }
       }
       unsigned long long nrows = 1;
@@ -673,8 +696,8 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
               const float avail = tup * (1.0f + 1.0f / 16384.0f) - lbs;
               const float g = sqrtf(fmaxf(avail, 0.0f)) * (1.0f + 1.0f / 1048576.0f);
               const float slack = (fabsf(qf[0]) + g) * (1.0f / 2097152.0f);
-              const uint32_t a0 = clamped_cell((T)(qf[0] - g - slack), p.g.minv[0], p.g.width, p.g.ncell[0]);
-              const uint32_t b0 = clamped_cell((T)(qf[0] + g + slack), p.g.minv[0], p.g.width, p.g.ncell[0]);
+              const uint32_t a0 = ring_cell(qf[0] - g - slack, s_minf[0], s_invw, p.g.ncell[0], false);
+              const uint32_t b0 = ring_cell(qf[0] + g + slack, s_minf[0], s_invw, p.g.ncell[0], true);
               xl = max(xl, a0);
               xh = min(xh, b0);
               empty = xl > xh;
