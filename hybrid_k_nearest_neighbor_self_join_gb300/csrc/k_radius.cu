@@ -178,14 +178,17 @@ void launch_mlp_tc(const Src& src, const float* model, uint64_t n, uint32_t* err
 // start with: keeps a ring at most ~1024 rows; growth beyond is handled by
 // the retry schedule and grid rebuilds.
 double learned_max_cells(uint32_t di) {
+  if (const char* e = std::getenv("KNNSJ_LEARNED_MAX_CELLS")) {  // tuning override
+    const double v = std::atof(e);
+    if (v >= 1.0) return v;
+  }
   switch (di) {
     case 1: return 64.0;
     case 2: return 64.0;
     case 3: return 15.0;
-    case 4: return 4.0;
-    case 5: return 2.0;
-    case 6: return 1.5;
-    default: return 1.0;
+    default: return 1.0;  // beyond three indexed dimensions a larger first ring
+                          // costs more than the passes it saves (measured on
+                          // 4-D and 6-D mixtures): large radii grow in retries
   }
 }
 
