@@ -50,6 +50,7 @@ knnsj_status make_config(const knnsj_options* o, uint32_t d, JoinConfig* c) {
   if (const char* e = env("KNNSJ_VERBOSE")) c->verbose = std::atoi(e);
   if (const char* e = env("KNNSJ_DENSE")) c->dense_mode = std::atoi(e);
   if (const char* e = env("KNNSJ_GRAPH")) c->use_graph = std::atoi(e);
+  if (const char* e = env("KNNSJ_FLOAT_PREFILTER")) c->float_prefilter = std::atoi(e);
   if (const char* e = env("KNNSJ_SEARCH_SHAPE")) {  // "warps,qchunk,buffer" (0 = default)
     int a = 0, b = 0, bb = 0;
     if (std::sscanf(e, "%d,%d,%d", &a, &b, &bb) >= 1) {

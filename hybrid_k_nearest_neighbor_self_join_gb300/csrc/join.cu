@@ -43,7 +43,7 @@ void* Arena::take(size_t bytes) {
 }
 
 void Workspace::attach_arena(Arena* a) {
-  DevBuf* bufs[] = {&model, &in, &ids, &dists, &xs, &ps, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
+  DevBuf* bufs[] = {&model, &in, &ids, &dists, &xs, &ps, &psf, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
                     &scan_tmp, &flags, &pos, &ckeys, &coff, &dstart, &list0, &list1, &small,
                     &eps_partial, &eps_sample, &perm, &minmax_part, &qradius};
   for (DevBuf* b : bufs) {
@@ -95,7 +95,7 @@ Workspace& workspace(int device) {
 
 void Workspace::release_all() {
   model_version = 0;
-  DevBuf* bufs[] = {&model, &in, &ids, &dists, &xs, &ps, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
+  DevBuf* bufs[] = {&model, &in, &ids, &dists, &xs, &ps, &psf, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
                     &scan_tmp, &flags, &pos, &ckeys, &coff, &dstart, &list0, &list1, &small,
                     &eps_partial, &eps_sample, &perm, &minmax_part, &qradius};
   for (DevBuf* b : bufs) b->release();
@@ -206,14 +206,16 @@ static void build_grid(Workspace& w, const JoinConfig& cfg, uint64_t n, uint32_t
   SmallDev* sm = (SmallDev*)w.small.p;
   launch_compact_cells(skeys, n, flags, pos, sc.scan_tmp, ckeys, coff, &sm->C, s);
   T* ps = (T*)w.ps.get(n * d * sizeof(T));
+  float* psf = sizeof(T) == 8 ? (float*)w.psf.get(n * d * sizeof(float)) : nullptr;
   uint32_t* pid = (uint32_t*)w.pid.get(n * 4);
   KNNSJ_CUDA(cudaMemcpyAsync(pid, sids, n * 4, cudaMemcpyDeviceToDevice, s));
-  launch_gather_sorted<T>(xs, n, d, sids, ps, s);
+  launch_gather_sorted<T>(xs, n, d, sids, ps, psf, s);
   unsigned long long C = 0;
   KNNSJ_CUDA(cudaMemcpyAsync(&C, &sm->C, sizeof(C), cudaMemcpyDeviceToHost, s));
   KNNSJ_CUDA(cudaStreamSynchronize(s));
   out->geom = g;
   out->ps = ps;
+  out->psf = psf;
   out->pid = pid;
   out->ckeys = ckeys;
   out->coff = coff;
@@ -320,6 +322,7 @@ struct Prepared {
   T eps0 = 0;
   int bucket = -1;
   double avg = 0.0;
+  double max_abs = 0.0;  // largest |coordinate| over all dimensions
   std::vector<T> mn, mx;
 };
 
@@ -382,6 +385,7 @@ static void prepare(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T
   double max_abs = 0.0;
   for (uint32_t j = 0; j < 2 * d; j++) max_abs = std::max(max_abs, std::fabs((double)hmm[j]));
   const double abs_err = sizeof(T) == 8 ? std::sqrt((double)d) * std::ldexp(max_abs, -22) : 0.0;
+  P->max_abs = max_abs;
   // buckets [0, 256) first; the rest only if the crossing lies beyond
   std::vector<uint32_t> hh(10000, 0);
   const uint32_t first_range = 256;
@@ -572,6 +576,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   a.shape.warps_per_block = cfg.search_warps;
   a.shape.qchunk = cfg.search_qchunk;
   a.shape.buffer = cfg.search_buffer;
+  a.coord_bound = cfg.float_prefilter ? P.max_abs : INFINITY;
   T r = P.eps0;
   const double step = (double)P.eps0 * 0.5;
   a.step = (T)step;

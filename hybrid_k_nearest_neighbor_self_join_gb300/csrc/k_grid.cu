@@ -263,11 +263,15 @@ __global__ void dense_table_kernel(const unsigned long long* __restrict__ ckeys,
 
 template <typename T>
 __global__ void gather_sorted_kernel(const T* __restrict__ soa, uint64_t n, uint32_t d,
-                                     const uint32_t* __restrict__ ids, T* __restrict__ ps) {
+                                     const uint32_t* __restrict__ ids, T* __restrict__ ps, float* __restrict__ psf) {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t src = ids[i];
-    for (uint32_t j = 0; j < d; j++) ps[(uint64_t)j * n + i] = soa[(uint64_t)j * n + src];
+    for (uint32_t j = 0; j < d; j++) {
+      const T v = soa[(uint64_t)j * n + src];
+      ps[(uint64_t)j * n + i] = v;
+      if (psf) psf[(uint64_t)j * n + i] = (float)v;  // round to nearest
+    }
   }
 }
 
@@ -337,9 +341,9 @@ void launch_dense_table(const unsigned long long* ckeys, const uint32_t* coff, u
 }
 
 template <typename T>
-void launch_gather_sorted(const T* soa, uint64_t n, uint32_t d, const uint32_t* sorted_ids, T* ps,
+void launch_gather_sorted(const T* soa, uint64_t n, uint32_t d, const uint32_t* sorted_ids, T* ps, float* psf,
                           cudaStream_t s) {
-  gather_sorted_kernel<T><<<grid_blocks(n), 256, 0, s>>>(soa, n, d, sorted_ids, ps);
+  gather_sorted_kernel<T><<<grid_blocks(n), 256, 0, s>>>(soa, n, d, sorted_ids, ps, psf);
   KNNSJ_CHECK_LAUNCH();
 }
 
@@ -347,9 +351,9 @@ template void launch_cell_ids<float>(const float*, uint64_t, const GridGeom<floa
                                      uint32_t*, cudaStream_t);
 template void launch_cell_ids<double>(const double*, uint64_t, const GridGeom<double>&, unsigned long long*,
                                       uint32_t*, cudaStream_t);
-template void launch_gather_sorted<float>(const float*, uint64_t, uint32_t, const uint32_t*, float*,
+template void launch_gather_sorted<float>(const float*, uint64_t, uint32_t, const uint32_t*, float*, float*,
                                           cudaStream_t);
-template void launch_gather_sorted<double>(const double*, uint64_t, uint32_t, const uint32_t*, double*,
+template void launch_gather_sorted<double>(const double*, uint64_t, uint32_t, const uint32_t*, double*, float*,
                                            cudaStream_t);
 
 }  // namespace knnsj

@@ -35,6 +35,8 @@
 // the rounding of the computed distance.  An accepted query's K rows are its
 // exact K nearest by (computed distance, id) -- the oracle's definition.
 
+#include <cmath>
+
 #include "knnsj_internal.h"
 
 namespace knnsj {
@@ -90,6 +92,11 @@ constexpr int wave_rows() {
 }
 constexpr uint32_t HIST_MAX_B = 256;  // histogram reduce for buffers up to this size
 constexpr int WARP_WORDS = 256 + 2 * MAX_RUNS + 8;  // per-warp u32 scratch: bins, runS, runP
+constexpr int FILTER_QUEUE = 64;  // double data: candidates that passed the float prefilter
+template <typename T>
+constexpr int warp_words() {
+  return WARP_WORDS + (sizeof(T) == 8 ? FILTER_QUEUE : 0);
+}
 
 template <typename T>
 struct SearchParams {
@@ -120,6 +127,8 @@ struct SearchParams {
   unsigned long long* cand_count;
   uint32_t* work_counter;
   FailRadii* fail_radii;
+  const float* __restrict__ psf;  // double data: float copy of ps for the prefilter (nullptr: off)
+  float filt_e1;                  // bound of the distance change from rounding coordinates to float
 };
 
 __device__ __forceinline__ unsigned long long lower_bound_u64(const unsigned long long* __restrict__ a,
@@ -469,12 +478,12 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   KT* buf = reinterpret_cast<KT*>(smem) + (size_t)wib * p.B;
-  uint32_t* words = reinterpret_cast<uint32_t*>(reinterpret_cast<KT*>(smem) + (size_t)wpb * p.B) + wib * WARP_WORDS;
+  uint32_t* words = reinterpret_cast<uint32_t*>(reinterpret_cast<KT*>(smem) + (size_t)wpb * p.B) + wib * warp_words<T>();
   uint32_t* hist = words;                   // [256]: reduce bins / output counting sort
   uint32_t* runS = words + 256;             // [MAX_RUNS]
   uint32_t* runP = words + 256 + MAX_RUNS;  // [MAX_RUNS + 1]
   T* qsm = reinterpret_cast<T*>(reinterpret_cast<uint32_t*>(reinterpret_cast<KT*>(smem) + (size_t)wpb * p.B) +
-                                wpb * WARP_WORDS) +
+                                wpb * warp_words<T>()) +
            (size_t)wib * MAX_D;
   const uint64_t n = p.n;
   const uint32_t di = DI > 0 ? (uint32_t)DI : p.g.di;
@@ -727,8 +736,93 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
         nr = WAVE_ROWS;
         w0 += wave;
         __syncwarp();
-        // the scan: one squared distance per lane, ballot-append under tau
         int row = 0;
+        if constexpr (sizeof(T) == 8) {
+          if (p.psf) {
+            // double data: float squared distances first; only candidates
+            // under the float bound (queued in shared memory) get the exact
+            // double distance, 32 at a time
+            uint32_t* queue = words + WARP_WORDS;
+            auto filt_thr = [&]() -> float {
+              const double t = (double)Kt::acc(st.tau);
+              const double sq = sqrt(t * (1.0 + 1.0 / 1099511627776.0)) + (double)p.filt_e1;
+              return __double2float_ru((1.0 + (double)(p.d + 4) * 1.1920928955078125e-07) * sq * sq);
+            };
+            float tf = filt_thr();
+            uint32_t qn = 0;
+            auto exact_batch = [&](uint32_t cnt_q, uint32_t base_q) {
+              bool pass = false;
+              KT key = Kt::maxv();
+              if (lane < cnt_q) {
+                const uint32_t j = queue[base_q + lane];
+                T acc = 0;
+                if (D > 0) {
+#pragma unroll
+                  for (int l = 0; l < (D > 0 ? D : 1); l++) {
+                    const T t = Num<T>::sub(p.ps[(uint64_t)l * n + j], q[l]);
+                    acc = Num<T>::fma(t, t, acc);
+                  }
+                } else {
+                  for (uint32_t l = 0; l < p.d; l++) {
+                    const T t = Num<T>::sub(p.ps[(uint64_t)l * n + j], qsm[l]);
+                    acc = Num<T>::fma(t, t, acc);
+                  }
+                }
+                if (acc <= Kt::acc(st.tau)) {
+                  key = Kt::make(acc, p.pid[j]);
+                  pass = Kt::less(key, st.tau);
+                }
+              }
+              const unsigned m = __ballot_sync(FULL, pass);
+              if (m) {
+                if (pass) buf[st.len + __popc(m & lanemask_lt())] = key;
+                st.len += __popc(m);
+                if (st.len > B - 32) {
+                  st = reduce<T>(buf, hist, st, K, B, lane);
+                  tf = filt_thr();
+                }
+              }
+            };
+            for (uint32_t v0 = 0; v0 < total; v0 += 32) {
+              const uint32_t v = v0 + lane;
+              bool surv = false;
+              uint32_t j = 0;
+              if (v < total) {
+                while (row < nr - 1 && runP[row + 1] <= v) row++;
+                j = runS[row] + (v - runP[row]);
+                float af = 0.0f;
+                if (D > 0) {
+#pragma unroll
+                  for (int l = 0; l < (D > 0 ? D : 1); l++) {
+                    const float t = __fsub_rn(p.psf[(uint64_t)l * n + j], (float)q[l]);
+                    af = __fmaf_rn(t, t, af);
+                  }
+                } else {
+                  for (uint32_t l = 0; l < p.d; l++) {
+                    const float t = __fsub_rn(p.psf[(uint64_t)l * n + j], (float)qsm[l]);
+                    af = __fmaf_rn(t, t, af);
+                  }
+                }
+                surv = af <= tf;
+              }
+              const unsigned m = __ballot_sync(FULL, surv);
+              if (surv) queue[qn + __popc(m & lanemask_lt())] = j;
+              qn += __popc(m);
+              __syncwarp();
+              if (qn >= 32) {
+                exact_batch(32, qn - 32);
+                qn -= 32;
+                __syncwarp();
+              }
+            }
+            if (qn) exact_batch(qn, 0);
+            scanned += total;
+            __syncwarp();
+            if (tighten && !st.tight && st.len >= K) st = reduce<T>(buf, hist, st, K, B, lane);
+            continue;
+          }
+        }
+        // the scan: one squared distance per lane, ballot-append under tau
         for (uint32_t v0 = 0; v0 < total; v0 += 32) {
           const uint32_t v = v0 + lane;
           bool pass = false;
@@ -810,7 +904,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
 template <typename T, int D, int DI>
 void launch_one(const SearchParams<T>& prm, int wpb_req, int sm_count, cudaStream_t s) {
   // per-warp shared memory: selection buffer, u32 scratch, query copy (generic d)
-  const size_t per_warp = (size_t)prm.B * sizeof(typename Key<T>::type) + WARP_WORDS * 4 +
+  const size_t per_warp = (size_t)prm.B * sizeof(typename Key<T>::type) + warp_words<T>() * 4 +
                           (D == 0 ? (size_t)MAX_D * sizeof(T) : 0);
   int wpb = SEARCH_THREADS / 32;
   if (wpb_req > 0 && wpb_req < wpb) wpb = wpb_req;
@@ -879,6 +973,19 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s) {
   p.cand_count = a.cand_count;
   p.work_counter = a.work_counter;
   p.fail_radii = a.fail_radii;
+  // Float prefilter for double data: a candidate is skipped when its float
+  // squared distance exceeds a bound that every candidate within the radius
+  // respects.  Rounding coordinates of magnitude <= M to float moves a
+  // distance by at most sqrt(d) * M * 2^-23 (plus subnormal slack).  Off
+  // when the coordinates could overflow a float square.
+  p.psf = nullptr;
+  p.filt_e1 = 0.0f;
+  if (sizeof(T) == 8 && a.grid.psf && std::isfinite(a.coord_bound) &&
+      2.0 * std::sqrt((double)a.d) * a.coord_bound < 1e18) {
+    p.psf = a.grid.psf;
+    const double e1 = std::sqrt((double)a.d) * (a.coord_bound * std::ldexp(1.0, -23) + std::ldexp(1.0, -140));
+    p.filt_e1 = (float)(e1 * (1.0 + 1e-6));
+  }
   KNNSJ_CUDA(cudaMemsetAsync(a.work_counter, 0, sizeof(uint32_t), s));
   const bool full = a.grid.geom.di == a.d;  // every dimension indexed
   switch (a.d) {

@@ -27,6 +27,7 @@ struct JoinConfig {
   double radius_offset = 0.0;  // added to the learned log-radius
   unsigned long long dense_cells_cap = 0;  // largest grid given a dense cell table; 0 = default
   int use_graph = 1;                       // retry passes after the first inside a CUDA graph
+  int float_prefilter = 1;                 // double data: float distances screen candidates first
   int search_warps = 0;                    // search launch shape (0 = default), see SearchShape
   int search_qchunk = 0;
   int search_buffer = 0;

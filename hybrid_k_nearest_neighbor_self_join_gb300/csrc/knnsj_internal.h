@@ -61,6 +61,7 @@ template <typename T>
 struct DeviceGrid {
   GridGeom<T> geom;
   const T* ps = nullptr;                  // SoA coords in cell order: d x n
+  const float* psf = nullptr;             // the same rounded to float (double data only)
   const uint32_t* pid = nullptr;          // original id of each sorted position
   const unsigned long long* ckeys = nullptr;  // sorted non-empty cell ids [C]
   const uint32_t* coff = nullptr;         // first sorted position of each cell [C+1]
@@ -123,7 +124,9 @@ void launch_dense_table(const unsigned long long* ckeys, const uint32_t* coff,
                         unsigned long long C, unsigned long long total_cells, uint32_t* dstart,
                         cudaStream_t s);
 template <typename T>
-void launch_gather_sorted(const T* soa, uint64_t n, uint32_t d, const uint32_t* sorted_ids, T* ps,
+// psf (optional): the same columns rounded to float (double data: the
+// search's float prefilter)
+void launch_gather_sorted(const T* soa, uint64_t n, uint32_t d, const uint32_t* sorted_ids, T* ps, float* psf,
                           cudaStream_t s);
 
 // ---- range search with fused top-K --------------------------------------
@@ -185,6 +188,7 @@ struct SearchLaunch {
   unsigned long long* cand_count = nullptr;
   uint32_t* work_counter = nullptr;
   FailRadii* fail_radii = nullptr;          // grown radii of the failures (per-query radii)
+  double coord_bound = 0.0;                 // largest |coordinate|: enables the float prefilter when finite
   SearchShape shape;                        // launch shape (autotuned for batched joins)
   const LoopCtl* ctl = nullptr;             // non-null: nq, lists and radius come from here (graph passes)
 };
@@ -197,7 +201,7 @@ struct Workspace {
   DevBuf model;                          // radius model (learned starting radius)
   unsigned model_version = 0;
   DevBuf in, ids, dists;                 // staging for host-pointer calls
-  DevBuf xs, ps, pid;                    // input-order columns, cell-order columns, ids
+  DevBuf xs, ps, psf, pid;               // input-order columns, cell-order columns (+ float copy), ids
   DevBuf keys0, keys1, vals0, vals1, hist, scan_tmp, flags, pos;  // grid build
   DevBuf ckeys, coff, dstart;            // cell tables
   DevBuf list0, list1, small, eps_partial, eps_sample, perm, minmax_part, qradius;
