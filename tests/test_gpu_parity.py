@@ -112,6 +112,16 @@ def test_double_2d():
     gpu_vs_oracle(x, 20, 2, 0.1)
 
 
+@pytest.mark.parametrize("offset", [0.0, 3.0e5])
+def test_double_float_prefilter_bound(offset):
+    # double data far from the origin: rounding the coordinates to float moves
+    # distances by more than the distances themselves, so the float prefilter
+    # must let every candidate through to the exact double test; near the
+    # origin it rejects most of them.  Both must keep the oracle's rows.
+    x = datasets.gmm(30_000, 4, 8, 0.2, 22, dtype=np.float64) * 1e-3 + offset
+    gpu_vs_oracle(x, 12, 4, 0.05)
+
+
 def test_dense_and_sparse_cell_lookup_agree(monkeypatch):
     x = datasets.sky_like(100_000, seed=13)
     monkeypatch.setenv("KNNSJ_DENSE", "0")
