@@ -36,6 +36,7 @@ namespace {
 constexpr int EPS_BLOCK = 256;
 constexpr uint32_t NBUCKETS = 10000;
 constexpr uint32_t EPS_CHUNK = 256;
+constexpr uint32_t HIST_SPLIT = 4;  // blocks per histogram sample point
 
 // One squared-distance term as the reference's double accumulator receives
 // it: a float product widened (no contraction across the type change) or a
@@ -146,13 +147,17 @@ __global__ void __launch_bounds__(EPS_BLOCK) eps_hist_kernel(const T* __restrict
                                                              uint32_t offset, const double* __restrict__ avg_in,
                                                              uint32_t* __restrict__ hist, uint32_t b_lo,
                                                              uint32_t b_hi, double abs_err) {
-  __shared__ uint32_t sh[NBUCKETS];
+  extern __shared__ uint32_t sh[];  // the b_hi - b_lo counted buckets
   const uint32_t nb = b_hi - b_lo;
   for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
   __syncthreads();
   const double avg = avg_in[0];
   const double bw = __ddiv_rn(avg, NBUCKETS * 1.0);  // GPU.cu:3356
-  const uint64_t sid = (uint64_t)blockIdx.x * offset;
+  // HIST_SPLIT blocks share one sample point, each taking every
+  // HIST_SPLIT-th round of candidates (integer counts: the order of the
+  // additions does not matter)
+  const uint64_t sid = (uint64_t)(blockIdx.x / HIST_SPLIT) * offset;
+  const uint32_t part = blockIdx.x % HIST_SPLIT;
   const float inv_bw = (float)(1.0 / bw);
   const float errc = (float)(2 * d + 8) * 5.9604645e-8f;  // (2d+8) * 2^-24, relative
   const float abs_q = (float)(abs_err / bw) * 1.0001f + 1e-4f;
@@ -164,7 +169,7 @@ __global__ void __launch_bounds__(EPS_BLOCK) eps_hist_kernel(const T* __restrict
   __syncthreads();
   constexpr uint64_t STEP = (uint64_t)EPS_BLOCK * 8;
   constexpr int U = 4;
-  for (uint64_t i0 = 0; i0 < n; i0 += STEP * U) {
+  for (uint64_t i0 = (uint64_t)part * STEP * U; i0 < n; i0 += STEP * U * HIST_SPLIT) {
     float s4[U];
 #pragma unroll
     for (int u = 0; u < U; u++) s4[u] = 0.0f;
@@ -256,7 +261,10 @@ void launch_eps_hist(const T* soa, uint64_t n, uint32_t d, const EpsScratch& sc,
   const uint32_t offset = eps_sample_offset(n);
   const uint32_t blocks2 = (uint32_t)n / offset;  // GPU.cu:3440 (integer division)
   if (blocks2 > 0 && b_hi > b_lo) {
-    eps_hist_kernel<T><<<blocks2, EPS_BLOCK, 0, s>>>(soa, n, d, offset, sc.avg_out, sc.hist, b_lo, b_hi, abs_err);
+    // shared memory for the counted bucket range only (256 buckets on the
+    // first try: a small footprint lets more blocks share an SM)
+    eps_hist_kernel<T><<<blocks2 * HIST_SPLIT, EPS_BLOCK, (size_t)(b_hi - b_lo) * 4, s>>>(
+        soa, n, d, offset, sc.avg_out, sc.hist, b_lo, b_hi, abs_err);
     KNNSJ_CHECK_LAUNCH();
   }
 }
