@@ -37,6 +37,9 @@ constexpr int EPS_BLOCK = 256;
 constexpr uint32_t NBUCKETS = 10000;
 constexpr uint32_t EPS_CHUNK = 256;
 constexpr uint32_t HIST_SPLIT = 4;  // blocks per histogram sample point
+#ifndef KNNSJ_EPS_UNROLL
+#define KNNSJ_EPS_UNROLL 4
+#endif
 
 // One squared-distance term as the reference's double accumulator receives
 // it: a float product widened (no contraction across the type change) or a
@@ -78,9 +81,9 @@ __global__ void eps_avg_chunk_kernel(const T* __restrict__ soa, uint64_t n, uint
   if (tid < n) {
     const uint64_t t = g % EPS_BLOCK;
     const uint64_t m_end = min(terms_of_sample(g, n), (uint64_t)(c + 1) * EPS_CHUNK);
-    // four terms at a time: their loads are independent; the sum still runs
-    // term by term in ascending order
-    constexpr int U = 4;
+    // U terms at a time: their loads and square roots are independent; the
+    // sum still runs term by term in ascending order
+    constexpr int U = KNNSJ_EPS_UNROLL;
     for (uint64_t m = (uint64_t)c * EPS_CHUNK; m < m_end; m += U) {
       double rd[U];
       {
