@@ -279,6 +279,31 @@ __host__ __device__ inline double median_fail_radius(const uint32_t* hist, uint3
   return rmax;
 }
 
+// Every ring stays within MAX_RING_ROWS rows, whatever the spread of the
+// per-query radii (rows are indexed in 32 bits and each one is visited): a
+// grid of width w serves radii up to w * ring_div / 2, whose rings span at
+// most ring_div + 3 cells per dimension, and a larger radius forces a
+// rebuild sized for it.  A single row (one indexed dimension) needs no cap.
+constexpr double MAX_RING_ROWS = 1048576.0;
+static double ring_div_of(uint32_t di) {
+  if (di <= 1) return 0.0;
+  return std::max(std::pow(MAX_RING_ROWS, 1.0 / (double)(di - 1)) - 3.0, 1.0);
+}
+__host__ __device__ inline bool ring_too_wide(double rmax, double width, double ring_div) {
+  return ring_div > 0.0 && rmax > 0.5 * width * ring_div;
+}
+
+// The radius the next grid is sized for and whether a rebuild is due, from
+// the radius the grid should suit (rgrid) and the largest radius in flight.
+__host__ __device__ inline bool regrid_due(double& rgrid, double rmax, double r_limit, double width,
+                                           double ring_div) {
+  if (ring_too_wide(rmax, width, ring_div)) {
+    rgrid = fmax(rgrid, 2.0 * rmax / ring_div);
+    return true;
+  }
+  return rgrid > r_limit && rgrid > width;
+}
+
 namespace {
 
 // One pass's bookkeeping inside the retry graph, mirroring the host loop of
@@ -307,7 +332,7 @@ __global__ void loop_step_kernel(LoopCtl* c, const uint32_t* __restrict__ fail_c
     }
     c->rmax_seen = fmax(c->rmax_seen, c->rmax);
   }
-  const bool regrid = c->rgrid > c->r_limit && c->rgrid > c->width;
+  const bool regrid = regrid_due(c->rgrid, c->rmax, c->r_limit, c->width, c->ring_div);
   cudaGraphSetConditional(handle, (nfail > 0 && c->iter < c->stop_iter && !regrid) ? 1u : 0u);
 }
 
@@ -589,6 +614,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   for (int b = 0; b < FAIL_RADIUS_BINS; b++) redge[b] = (double)P.eps0 * std::exp2((b - 15) / 4.0);
   const int max_iter = cfg.max_iterations > 0 ? cfg.max_iterations : 100000;
   double r_limit = regrid_limit((double)a.grid.geom.width, di);
+  const double ring_div = ring_div_of(di);
   // passes after the first run inside a CUDA graph (no host round trip per
   // pass) unless the stream cannot be captured (the legacy default stream)
   bool graph_ok = cfg.use_graph && s != nullptr && ev[4] != nullptr && cfg.verbose < 2;
@@ -598,7 +624,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     // learned starting radii are clamped so their rings stay small on the
     // eps0 grid: no rebuild for the first pass
     const bool first_learned = qrad && iter == 0;
-    if (!first_learned && rgrid > r_limit && rgrid > (double)a.grid.geom.width) {
+    if (!first_learned && regrid_due(rgrid, rmax, r_limit, (double)a.grid.geom.width, ring_div)) {
       // coarser grid for the radius in flight (like main.cu:333-356); the
       // widened width keeps that radius's ring at three cells per dimension
       const T wnew = (T)(rgrid * (1.0 + 1.0 / 32768.0));
@@ -623,6 +649,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
       c.r_limit = r_limit;
       c.width = (double)a.grid.geom.width;
       c.per_query = qrad ? 1 : 0;
+      c.ring_div = ring_div;
       if (run_graph_passes<T>(a, c, dctl, sm, w.sm_count, s, ev[4], ev[5], &kernel_ms)) {
         const int passes = (int)c.iter - iter;
         // the capture counted the search and step kernels once; each pass ran both

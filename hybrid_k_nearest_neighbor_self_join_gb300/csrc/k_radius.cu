@@ -174,6 +174,8 @@ void launch_mlp_tc(const Src& src, const float* model, uint64_t n, uint32_t* err
 
 }  // namespace
 
+constexpr float LEARNED_LOG_MARGIN = 0.08f;
+
 // Largest ring half-width (in cells of the eps0 grid) a learned radius may
 // start with: keeps a ring at most ~1024 rows; growth beyond is handled by
 // the retry schedule and grid rebuilds.
@@ -205,6 +207,10 @@ void launch_radius_assign(const DeviceGrid<T>& g, uint64_t n, uint32_t d, uint32
                           cudaStream_t s) {
   const float log_lo = std::log(1.0f / 16.0f);
   const float log_hi = (float)std::log(learned_max_cells(g.geom.di) * (1.0 - 1.0 / 4096.0));
+  // the model predicts the 0.9 quantile of log(r_K / eps0); a failed first
+  // pass costs a second scan at a larger radius, so starting 8% wider (in
+  // radius) is cheaper overall (measured on 2-D, 3-D and 4-D joins, k 32-64)
+  offset += LEARNED_LOG_MARGIN;
   if (mlp_on_tensor_cores()) {
     AssignSrc<T> src{table_of(g), g.ps, g.pid, n, d, k, beta, (float)eps0, log_lo, log_hi, offset, qradius};
     launch_mlp_tc(src, d_model, n, d_err, sm_count, s);

@@ -62,11 +62,6 @@ constexpr int QCHUNK = 4;            // default queries per work fetch
 #ifndef KNNSJ_SORT_ROWS
 #define KNNSJ_SORT_ROWS 1
 #endif
-// rings of at most this many rows are scanned in their natural order (one or
-// two waves: sorting them by lower bound saves nothing)
-#ifndef KNNSJ_SORT_MIN_ROWS
-#define KNNSJ_SORT_MIN_ROWS 4
-#endif
 // intermediate threshold tightening once K keys are held: 0 only when the
 // buffer fills, 1 after every wave, 2 after every wave for a uniform radius
 // only (a per-query starting radius is already close to the K-th distance)
@@ -614,7 +609,9 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
       // wave being the query's own row alone), so rows are visited nearest
       // first; per-query radii are already close to the K-th distance
       const bool tighten = KNNSJ_TIGHTEN == 1 || (KNNSJ_TIGHTEN == 2 && p.qradius == nullptr);
-      const bool sorted_rows = KNNSJ_SORT_ROWS && (nrows > KNNSJ_SORT_MIN_ROWS || (tighten && nrows > 1));
+      // rows are sorted when a later wave can be pruned: with a per-query
+      // radius a ring of one wave is scanned in its natural order
+      const bool sorted_rows = KNNSJ_SORT_ROWS && (tighten ? nrows > 1 : nrows > (unsigned long long)WAVE_ROWS);
 
       bool fail_now = false;
       uint32_t ring_cnt = 0;  // points in the ring's cells, when counted

@@ -151,6 +151,7 @@ struct LoopCtl {
   unsigned long long accepted;
   int per_query;       // per-query radii (learned starting radius)
   int pad;
+  double ring_div;     // radii above width * ring_div / 2 force a rebuild (0: none)
   double redge[64];    // upper radius of each bin of the failing-radius histogram
 };
 

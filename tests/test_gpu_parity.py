@@ -147,6 +147,22 @@ def test_graph_passes_match_host_passes(monkeypatch, mode):
         assert a_s[key] == b_s[key], key
 
 
+def test_far_outliers_rebuild_for_the_widest_ring():
+    # a tight 6-D cluster and a few far outliers: the outliers' radii grow
+    # far past the cluster's, so the grid is rebuilt for the largest radius
+    # (rings stay within the row cap); rows still match brute force
+    rng = np.random.default_rng(23)
+    c = rng.normal(0.0, 0.01, (40_000, 6)).astype(np.float32)
+    o = rng.uniform(-1.0, 1.0, (12, 6)).astype(np.float32)
+    x = np.concatenate([c, o])
+    ids, dists, st = kj.selfjoin(x, 16, beta=0.05, radius_mode=kj.RADIUS_LEARNED, return_stats=True)
+    assert st["regrids"] >= 1
+    perm, _ = kj.reorder_dims(x)
+    q = np.concatenate([np.arange(40_000, 40_012), np.arange(0, 40_000, 997)])
+    bi, bd = oracle.bruteforce(x[:, perm], 17, q)
+    assert_same(ids[q], dists[q], bi, bd)
+
+
 def test_tiny_input_eps_fallback():
     # N <= 1000: the reference's sampled mean distance is 0 and its grid
     # divides by zero; the GPU path picks a positive width and stays exact.
