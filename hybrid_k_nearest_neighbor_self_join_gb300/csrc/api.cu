@@ -51,6 +51,7 @@ knnsj_status make_config(const knnsj_options* o, uint32_t d, JoinConfig* c) {
   if (const char* e = env("KNNSJ_DENSE")) c->dense_mode = std::atoi(e);
   if (const char* e = env("KNNSJ_GRAPH")) c->use_graph = std::atoi(e);
   if (const char* e = env("KNNSJ_FLOAT_PREFILTER")) c->float_prefilter = std::atoi(e);
+  if (const char* e = env("KNNSJ_ROW_CHUNKS")) c->row_chunks = std::atoi(e);
   if (const char* e = env("KNNSJ_SEARCH_SHAPE")) {  // "warps,qchunk,buffer" (0 = default)
     int a = 0, b = 0, bb = 0;
     if (std::sscanf(e, "%d,%d,%d", &a, &b, &bb) >= 1) {
@@ -148,6 +149,9 @@ void init_stats(knnsj_stats* st) {
   st->struct_size = sz ? sz : (uint32_t)sizeof(*st);
 }
 
+// Outputs of fewer rows go back in one copy after the join.
+constexpr uint64_t ROW_STREAM_MIN_ROWS = 1u << 18;
+
 template <typename T>
 void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t k, const JoinConfig& cfg,
                   int32_t* out_ids, T* out_d, knnsj_stats* st, bool checksum) {
@@ -162,17 +166,47 @@ void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t 
   KNNSJ_CUDA(cudaEventRecord(t0, s));
   KNNSJ_CUDA(cudaMemcpyAsync(din, data, n * d * sizeof(T), cudaMemcpyHostToDevice, s));
   KNNSJ_CUDA(cudaEventRecord(t1, s));
-  run_join<T>(w, cfg, din, data, n, d, k, dids, ddist, st, s);
+  // pinned output buffers take their rows while the join runs
+  RowStream rs;
+  RowStream* rsp = nullptr;
+  if (cfg.row_chunks >= 2 && n >= ROW_STREAM_MIN_ROWS) {
+    cudaPointerAttributes ai{}, ad{};
+    if (cudaPointerGetAttributes(&ai, out_ids) == cudaSuccess && cudaPointerGetAttributes(&ad, out_d) == cudaSuccess &&
+        ai.type == cudaMemoryTypeHost && ad.type == cudaMemoryTypeHost && ai.devicePointer && ad.devicePointer) {
+      rs.ids_host = out_ids;
+      rs.d_host = out_d;
+      rs.ids_dev = ai.devicePointer;
+      rs.d_dev = ad.devicePointer;
+      rs.chunks = cfg.row_chunks;
+      rsp = &rs;
+    }
+    cudaGetLastError();  // an unregistered pointer is not an error here
+  }
+  struct CopyWait {  // no copy into the caller's buffers outlives this call
+    Workspace* w = nullptr;
+    ~CopyWait() {
+      if (!w) return;
+      cudaStreamSynchronize(w->copy_stream);
+      w->mail = false;
+    }
+  } copy_wait;
+  if (rsp) copy_wait.w = &w;
+  run_join<T>(w, cfg, din, data, n, d, k, dids, ddist, st, s, rsp);
+  // (the checksum runs while the last row copies are still in flight)
   if (st && checksum) st->total_distance = device_checksum<T>(w, ddist, n * K, s);
   cudaEvent_t t2, t3;
   KNNSJ_CUDA(cudaEventCreate(&t2));
   KNNSJ_CUDA(cudaEventCreate(&t3));
   KNNSJ_CUDA(cudaEventRecord(t2, s));
-  KNNSJ_CUDA(cudaMemcpyAsync(out_ids, dids, n * K * 4, cudaMemcpyDeviceToHost, s));
-  KNNSJ_CUDA(cudaMemcpyAsync(out_d, ddist, n * K * sizeof(T), cudaMemcpyDeviceToHost, s));
+  if (rsp && rsp->active) {
+    finish_row_stream<T>(w, *rsp, dids, ddist, (uint32_t)K, s);
+  } else {
+    KNNSJ_CUDA(cudaMemcpyAsync(out_ids, dids, n * K * 4, cudaMemcpyDeviceToHost, s));
+    KNNSJ_CUDA(cudaMemcpyAsync(out_d, ddist, n * K * sizeof(T), cudaMemcpyDeviceToHost, s));
+  }
   KNNSJ_CUDA(cudaEventRecord(t3, s));
   KNNSJ_CUDA(cudaStreamSynchronize(s));
-  if (st) {
+  if (st) {  // streamed rows: the copies that outlast the join
     float a = 0, b = 0;
     cudaEventElapsedTime(&a, t0, t1);
     cudaEventElapsedTime(&b, t2, t3);

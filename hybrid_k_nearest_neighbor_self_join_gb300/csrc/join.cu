@@ -45,7 +45,7 @@ void* Arena::take(size_t bytes) {
 void Workspace::attach_arena(Arena* a) {
   DevBuf* bufs[] = {&model, &in, &ids, &dists, &xs, &ps, &psf, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
                     &scan_tmp, &flags, &pos, &ckeys, &coff, &dstart, &list0, &list1, &small,
-                    &eps_partial, &eps_sample, &perm, &minmax_part, &qradius};
+                    &eps_partial, &eps_sample, &perm, &minmax_part, &qradius, &chunk_list, &patch_rows};
   for (DevBuf* b : bufs) {
     b->arena = a;
     b->p = nullptr;
@@ -97,14 +97,23 @@ void Workspace::release_all() {
   model_version = 0;
   DevBuf* bufs[] = {&model, &in, &ids, &dists, &xs, &ps, &psf, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
                     &scan_tmp, &flags, &pos, &ckeys, &coff, &dstart, &list0, &list1, &small,
-                    &eps_partial, &eps_sample, &perm, &minmax_part, &qradius};
+                    &eps_partial, &eps_sample, &perm, &minmax_part, &qradius, &chunk_list, &patch_rows};
   for (DevBuf* b : bufs) b->release();
   if (stream) cudaStreamDestroy(stream);
   stream = nullptr;
+  if (copy_stream) cudaStreamDestroy(copy_stream);
+  copy_stream = nullptr;
   for (auto& e : ev) {
     if (e) cudaEventDestroy(e);
     e = nullptr;
   }
+  for (auto& e : chunk_ev) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
+  if (mail_host) cudaFreeHost(mail_host);
+  mail_host = mail_dev = nullptr;
+  mail = false;
   pinned_release();
 }
 
@@ -129,6 +138,82 @@ void Workspace::ensure_stream() {
     if (!e) KNNSJ_CUDA(cudaEventCreate(&e));
 }
 
+void Workspace::ensure_copy_stream() {
+  if (!copy_stream) KNNSJ_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+  for (auto& e : chunk_ev)
+    if (!e) KNNSJ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  if (!mail_host) {
+    KNNSJ_CUDA(cudaHostAlloc(&mail_host, MAIL_BYTES, cudaHostAllocMapped));
+    KNNSJ_CUDA(cudaHostGetDevicePointer(&mail_dev, mail_host, 0));
+  }
+}
+
+namespace {
+
+__global__ void copy_words_kernel(uint32_t* __restrict__ dst, const uint32_t* __restrict__ src, uint64_t words) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+__global__ void zero_words_kernel(uint32_t* __restrict__ p, uint64_t words) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (uint64_t)gridDim.x * blockDim.x)
+    p[i] = 0u;
+}
+
+void launch_copy_words(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  const uint64_t words = bytes / 4;
+  const uint64_t blocks = std::min<uint64_t>((words + 255) / 256, 1024);
+  if (blocks == 0) return;
+  copy_words_kernel<<<(unsigned)blocks, 256, 0, s>>>((uint32_t*)dst, (const uint32_t*)src, words);
+  KNNSJ_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+void launch_zero_words(void* p, size_t bytes, cudaStream_t s) {
+  const uint64_t words = bytes / 4;
+  const uint64_t blocks = std::min<uint64_t>((words + 255) / 256, 1024);
+  if (blocks == 0) return;
+  zero_words_kernel<<<(unsigned)blocks, 256, 0, s>>>((uint32_t*)p, words);
+  KNNSJ_CHECK_LAUNCH();
+}
+
+// Device-to-device copy (bytes a multiple of 4).
+static void dev_copy(Workspace& w, void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (w.mail)
+    launch_copy_words(dst, src, bytes, s);
+  else
+    KNNSJ_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s));
+}
+
+// Device-to-host read of a few bytes (a multiple of 4); synchronises s.
+static void read_small(Workspace& w, void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (w.mail) {
+    if (bytes > MAIL_BYTES / 2) throw StatusError{KNNSJ_ERR_UNSUPPORTED, "mailbox read too large"};
+    launch_copy_words(w.mail_dev, src, bytes, s);
+    KNNSJ_CUDA(cudaStreamSynchronize(s));
+    std::memcpy(dst, w.mail_host, bytes);
+    return;
+  }
+  KNNSJ_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+  KNNSJ_CUDA(cudaStreamSynchronize(s));
+}
+
+// Host-to-device write of a few bytes (a multiple of 4); the source may be
+// reused on return.
+static void write_small(Workspace& w, void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (w.mail) {
+    if (bytes > MAIL_BYTES / 2) throw StatusError{KNNSJ_ERR_UNSUPPORTED, "mailbox write too large"};
+    unsigned char* in_host = (unsigned char*)w.mail_host + MAIL_BYTES / 2;
+    std::memcpy(in_host, src, bytes);
+    launch_copy_words(dst, (unsigned char*)w.mail_dev + MAIL_BYTES / 2, bytes, s);
+    KNNSJ_CUDA(cudaStreamSynchronize(s));  // the mailbox is free again
+    return;
+  }
+  KNNSJ_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+  KNNSJ_CUDA(cudaStreamSynchronize(s));
+}
+
 namespace {
 
 struct SmallDev {  // layout of Workspace::small
@@ -145,6 +230,8 @@ struct SmallDev {  // layout of Workspace::small
   FailRadii fr;
   LoopCtl ctl;
   uint32_t mlp_err;  // the tensor-core radius MLP timed out
+  uint32_t chunk_fill[MAX_ROW_CHUNKS];  // streamed rows: queries placed per id block
+  uint32_t patch_count;                 // streamed rows: first-pass failures
 };
 
 template <typename T>
@@ -208,11 +295,10 @@ static void build_grid(Workspace& w, const JoinConfig& cfg, uint64_t n, uint32_t
   T* ps = (T*)w.ps.get(n * d * sizeof(T));
   float* psf = sizeof(T) == 8 ? (float*)w.psf.get(n * d * sizeof(float)) : nullptr;
   uint32_t* pid = (uint32_t*)w.pid.get(n * 4);
-  KNNSJ_CUDA(cudaMemcpyAsync(pid, sids, n * 4, cudaMemcpyDeviceToDevice, s));
+  dev_copy(w, pid, sids, n * 4, s);
   launch_gather_sorted<T>(xs, n, d, sids, ps, psf, s);
   unsigned long long C = 0;
-  KNNSJ_CUDA(cudaMemcpyAsync(&C, &sm->C, sizeof(C), cudaMemcpyDeviceToHost, s));
-  KNNSJ_CUDA(cudaStreamSynchronize(s));
+  read_small(w, &C, &sm->C, sizeof(C), s);
   out->geom = g;
   out->ps = ps;
   out->psf = psf;
@@ -313,7 +399,8 @@ namespace {
 // pass and stop_iter is finite).
 template <typename T>
 __global__ void loop_step_kernel(LoopCtl* c, const uint32_t* __restrict__ fail_count,
-                                 const FailRadii* __restrict__ fr, cudaGraphConditionalHandle handle) {
+                                 const FailRadii* __restrict__ fr, cudaGraphConditionalHandle handle,
+                                 int in_graph) {
   const uint32_t nfail = *fail_count;
   c->queries_run += c->nq;
   c->accepted += c->nq - nfail;
@@ -333,7 +420,59 @@ __global__ void loop_step_kernel(LoopCtl* c, const uint32_t* __restrict__ fail_c
     c->rmax_seen = fmax(c->rmax_seen, c->rmax);
   }
   const bool regrid = regrid_due(c->rgrid, c->rmax, c->r_limit, c->width, c->ring_div);
-  cudaGraphSetConditional(handle, (nfail > 0 && c->iter < c->stop_iter && !regrid) ? 1u : 0u);
+  c->go = (nfail > 0 && c->iter < c->stop_iter && !regrid) ? 1 : 0;
+  if (in_graph) cudaGraphSetConditional(handle, c->go ? 1u : 0u);
+}
+
+// First node of the retry graph: the loop runs while the loop state says so.
+__global__ void loop_cond_kernel(const LoopCtl* c, cudaGraphConditionalHandle handle) {
+  cudaGraphSetConditional(handle, c->go ? 1u : 0u);
+}
+
+// Streamed rows: the queries of each block of crow consecutive ids, in the
+// cell order they have in pid (nearby queries stay together), block c at
+// lists[c * crow ...].  Lanes of a warp with the same block take consecutive
+// slots from one atomic.
+__global__ void chunk_lists_kernel(const uint32_t* __restrict__ pid, uint32_t n, uint32_t crow,
+                                   uint32_t* __restrict__ fill, uint32_t* __restrict__ lists) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool live = i < n;
+  const uint32_t id = live ? pid[i] : 0u;
+  const uint32_t c = live ? id / crow : 0xffffffffu;
+  const unsigned peers = __match_any_sync(0xffffffffu, c);
+  const int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (live && lane == leader) base = atomicAdd(&fill[c], (uint32_t)__popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (live) lists[(uint64_t)c * crow + base + __popc(peers & ((1u << lane) - 1u))] = id;
+}
+
+// Streamed rows: the first pass's failures (count on the device), kept for
+// the patch after the lists are reused by later passes.
+__global__ void save_fail_list_kernel(const uint32_t* __restrict__ src, const uint32_t* __restrict__ count,
+                                      uint32_t* __restrict__ dst, uint32_t* __restrict__ saved) {
+  const uint32_t nf = *count;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *saved = nf;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x) dst[i] = src[i];
+}
+
+// Streamed rows: rows finished after the first pass, copied from the device
+// table into the host buffers (one warp per row).
+template <typename T>
+__global__ void patch_rows_kernel(const uint32_t* __restrict__ rows, const uint32_t* __restrict__ count,
+                                  const int32_t* __restrict__ ids, const T* __restrict__ dists, uint32_t K,
+                                  int32_t* h_ids, T* h_d) {
+  const uint32_t nrows = *count;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t wid = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; wid < nrows; wid += nwarps) {
+    const uint64_t base = (uint64_t)rows[wid] * K;
+    for (uint32_t j = lane; j < K; j += 32) {
+      h_ids[base + j] = ids[base + j];
+      h_d[base + j] = dists[base + j];
+    }
+  }
 }
 
 }  // namespace
@@ -486,15 +625,36 @@ static double decode_radius(unsigned long long bits) {
 // Returns false, having run nothing, when conditional graph nodes are not
 // available.
 template <typename T>
-static bool run_graph_passes(SearchLaunch<T> a, LoopCtl& c, LoopCtl* dctl, SmallDev* sm, int sm_count,
-                             cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, double* kernel_ms) {
+static bool run_graph_passes(Workspace& w, SearchLaunch<T> a, LoopCtl& c, LoopCtl* dctl, SmallDev* sm,
+                             int sm_count, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, double* kernel_ms,
+                             bool upload = true, uint32_t iter_before = 0) {
+  // launches are counted as they ran: the body's once per pass, the
+  // condition node once
+  if (upload) iter_before = c.iter;
+  unsigned long long body = 0;
   cudaGraph_t g = nullptr;
   KNNSJ_CUDA(cudaGraphCreate(&g, 0));
   cudaGraphConditionalHandle h;
-  if (cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+  if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) {
     cudaGetLastError();
     cudaGraphDestroy(g);
     return false;
+  }
+  // the loop state decides whether the first pass runs at all
+  cudaGraphNode_t cond_node;
+  {
+    const LoopCtl* cp = dctl;
+    void* args[] = {(void*)&cp, (void*)&h};
+    cudaKernelNodeParams kp{};
+    kp.func = (void*)loop_cond_kernel;
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(1);
+    kp.kernelParams = args;
+    if (cudaGraphAddKernelNode(&cond_node, g, nullptr, 0, &kp) != cudaSuccess) {
+      cudaGetLastError();
+      cudaGraphDestroy(g);
+      return false;
+    }
   }
   // (the parameter union has no default constructor: zeroed raw storage)
   alignas(cudaGraphNodeParams) unsigned char np_raw[sizeof(cudaGraphNodeParams)];
@@ -505,38 +665,41 @@ static bool run_graph_passes(SearchLaunch<T> a, LoopCtl& c, LoopCtl* dctl, Small
   np->conditional.type = cudaGraphCondTypeWhile;
   np->conditional.size = 1;
   cudaGraphNode_t node;
-  if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, np) != cudaSuccess) {
+  if (cudaGraphAddNode(&node, g, &cond_node, nullptr, 1, np) != cudaSuccess) {
     cudaGetLastError();
     cudaGraphDestroy(g);
     return false;
   }
-  cudaGraph_t body = np->conditional.phGraph_out[0];
+  cudaGraph_t body_graph = np->conditional.phGraph_out[0];
   cudaGraphExec_t ex = nullptr;
   try {
-    KNNSJ_CUDA(cudaMemcpyAsync(dctl, &c, sizeof(LoopCtl), cudaMemcpyHostToDevice, s));
-    KNNSJ_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    if (upload) write_small(w, dctl, &c, sizeof(LoopCtl), s);
+    const unsigned long long l0 = g_launches;
+    KNNSJ_CUDA(cudaStreamBeginCaptureToGraph(s, body_graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     try {
       a.ctl = dctl;
       a.qlist = c.list[c.cur];  // placeholders: the kernel reads the live values from dctl
       a.fail_list = c.list[c.cur ^ 1];
       a.nq = c.nq;
-      KNNSJ_CUDA(cudaMemsetAsync(&sm->fail_count, 0, 4, s));
-      KNNSJ_CUDA(cudaMemsetAsync(&sm->fr, 0, sizeof(FailRadii), s));
+      launch_zero_words(&sm->fail_count, 4, s);
+      launch_zero_words(&sm->fr, sizeof(FailRadii), s);
       launch_search<T>(a, sm_count, s);
-      loop_step_kernel<T><<<1, 1, 0, s>>>(dctl, &sm->fail_count, &sm->fr, h);
+      loop_step_kernel<T><<<1, 1, 0, s>>>(dctl, &sm->fail_count, &sm->fr, h, 1);
       KNNSJ_CHECK_LAUNCH();
     } catch (...) {
       cudaGraph_t dummy = nullptr;
       cudaStreamEndCapture(s, &dummy);
       throw;
     }
-    KNNSJ_CUDA(cudaStreamEndCapture(s, &body));
+    KNNSJ_CUDA(cudaStreamEndCapture(s, &body_graph));
+    body = g_launches - l0;
     KNNSJ_CUDA(cudaGraphInstantiate(&ex, g, 0));
     KNNSJ_CUDA(cudaEventRecord(e0, s));
     KNNSJ_CUDA(cudaGraphLaunch(ex, s));
     KNNSJ_CUDA(cudaEventRecord(e1, s));
-    KNNSJ_CUDA(cudaMemcpyAsync(&c, dctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, s));
-    KNNSJ_CUDA(cudaStreamSynchronize(s));
+    read_small(w, &c, dctl, sizeof(LoopCtl), s);
+    const unsigned long long passes = c.iter - iter_before;
+    g_launches = g_launches - body + body * passes + 1;
   } catch (...) {
     if (ex) cudaGraphExecDestroy(ex);
     cudaGraphDestroy(g);
@@ -552,7 +715,7 @@ static bool run_graph_passes(SearchLaunch<T> a, LoopCtl& c, LoopCtl* dctl, Small
 
 template <typename T>
 void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
-              uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s) {
+              uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s, RowStream* rows) {
   const uint32_t K = k + 1;
   const uint32_t di = cfg.num_indexed_dims;
   cudaEvent_t* ev = w.ev;
@@ -619,6 +782,120 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   // pass) unless the stream cannot be captured (the legacy default stream)
   bool graph_ok = cfg.use_graph && s != nullptr && ev[4] != nullptr && cfg.verbose < 2;
   LoopCtl* dctl = &sm->ctl;
+
+  // 6a. streamed rows: the first pass in blocks of query ids, each block's
+  // rows copied into the host buffers while the next block searches.  The
+  // copies keep the host link busy, so the pass bookkeeping stays on the
+  // device (the step kernel, then the retry graph) with no host round trip
+  // until the graph stops.
+  // (the caller waits for the copies and patches the late rows in:
+  // finish_row_stream)
+  const bool streamed = rows && rows->chunks >= 2 && n >= (uint64_t)rows->chunks;
+  if (streamed) {
+    w.ensure_copy_stream();
+    w.mail = true;
+    rows->active = true;
+    const int C = std::min(rows->chunks, MAX_ROW_CHUNKS);
+    const uint32_t crow = (uint32_t)((n + C - 1) / C);
+    uint32_t* clist = (uint32_t*)w.chunk_list.get(n * 4);
+    const bool dev_loop = graph_ok;
+    LoopCtl c{};
+    c.nq = (uint32_t)n;
+    c.iter = 0;
+    c.cur = 0;
+    c.stop_iter = (uint32_t)std::min<int64_t>((int64_t)max_iter, 256);
+    c.list[0] = list[0];
+    c.list[1] = list[1];
+    c.r = (double)r;
+    c.step = step;
+    c.rmax = rmax;
+    c.rgrid = rgrid;
+    c.rmax_seen = rmax_seen;
+    for (int b = 0; b < FAIL_RADIUS_BINS; b++) c.redge[b] = redge[b];
+    c.r_limit = r_limit;
+    c.width = (double)a.grid.geom.width;
+    c.per_query = qrad ? 1 : 0;
+    c.ring_div = ring_div;
+    c.go = 0;
+    if (dev_loop) write_small(w, dctl, &c, sizeof(LoopCtl), s);
+    launch_zero_words(sm->chunk_fill, sizeof(sm->chunk_fill), s);
+    chunk_lists_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a.grid.pid, (uint32_t)n, crow, sm->chunk_fill,
+                                                                   clist);
+    KNNSJ_CHECK_LAUNCH();
+    launch_zero_words(&sm->fail_count, 4, s);
+    launch_zero_words(&sm->fr, sizeof(FailRadii), s);
+    a.radius = r;
+    a.fail_list = list[1];
+    KNNSJ_CUDA(cudaEventRecord(ev[6], s));
+    for (int ch = 0; ch < C; ch++) {
+      const uint64_t r0 = (uint64_t)ch * crow;
+      if (r0 >= n) break;
+      const uint64_t nr = std::min<uint64_t>(crow, n - r0);
+      a.qlist = clist + r0;
+      a.nq = (uint32_t)nr;
+      launch_search<T>(a, w.sm_count, s);
+      KNNSJ_CUDA(cudaEventRecord(w.chunk_ev[ch], s));
+      KNNSJ_CUDA(cudaStreamWaitEvent(w.copy_stream, w.chunk_ev[ch], 0));
+      KNNSJ_CUDA(cudaMemcpyAsync((int32_t*)rows->ids_host + r0 * K, d_ids + r0 * K, nr * K * 4,
+                                 cudaMemcpyDeviceToHost, w.copy_stream));
+      KNNSJ_CUDA(cudaMemcpyAsync((T*)rows->d_host + r0 * K, d_dists + r0 * K, nr * K * sizeof(T),
+                                 cudaMemcpyDeviceToHost, w.copy_stream));
+    }
+    KNNSJ_CUDA(cudaEventRecord(ev[7], s));
+    // the block lists are spent: they keep the failures for the patch
+    save_fail_list_kernel<<<(unsigned)(w.sm_count * 4), 256, 0, s>>>(list[1], &sm->fail_count, clist,
+                                                                    &sm->patch_count);
+    KNNSJ_CHECK_LAUNCH();
+    alg_bytes += (double)n * d * sizeof(T);  // the pass's candidate columns; the rest is counted below
+    bool ran = false;
+    if (dev_loop) {
+      loop_step_kernel<T><<<1, 1, 0, s>>>(dctl, &sm->fail_count, &sm->fr, 0, 0);
+      KNNSJ_CHECK_LAUNCH();
+      ran = run_graph_passes<T>(w, a, c, dctl, sm, w.sm_count, s, ev[4], ev[5], &kernel_ms, false, 1);
+      if (ran) {
+        const int passes = (int)c.iter - 1;
+        alg_bytes += (double)passes * n * d * sizeof(T);
+      } else {
+        graph_ok = false;
+        read_small(w, &c, dctl, sizeof(LoopCtl), s);
+      }
+    } else {  // host bookkeeping, as after any host-driven pass
+      uint32_t nfail = 0;
+      FailRadii fr{};
+      read_small(w, &nfail, &sm->fail_count, 4, s);
+      if (qrad) read_small(w, &fr, &sm->fr, sizeof(FailRadii), s);
+      c.queries_run = n;
+      c.accepted = n - nfail;
+      c.nq = nfail;
+      c.iter = 1;
+      c.cur = 1;
+      if (nfail > 0) {
+        if (qrad) {
+          c.rmax = decode_radius<T>(fr.rmax_bits);
+          c.rgrid = median_fail_radius(fr.hist, nfail, redge, c.rmax);
+        } else {
+          c.r = (double)(T)((double)r + step);  // main.cu:336
+          c.rmax = c.r;
+          c.rgrid = c.rmax;
+        }
+        c.rmax_seen = std::max(c.rmax_seen, c.rmax);
+      }
+    }
+    float first_ms = 0.f;
+    KNNSJ_CUDA(cudaEventSynchronize(ev[7]));
+    KNNSJ_CUDA(cudaEventElapsedTime(&first_ms, ev[6], ev[7]));
+    kernel_ms += first_ms;
+    alg_bytes += (double)c.queries_run * d * sizeof(T) + (double)c.accepted * K * (4.0 + sizeof(T));
+    queries_run += c.queries_run;
+    iter = (int)c.iter;
+    cur = (int)c.cur;
+    nq = c.nq;
+    r = (T)c.r;
+    rmax = c.rmax;
+    rgrid = c.rgrid;
+    rmax_seen = c.rmax_seen;
+  }
+
   while (nq > 0) {
     if (iter >= max_iter) throw StatusError{KNNSJ_ERR_NO_CONVERGENCE, "iteration cap reached"};
     // learned starting radii are clamped so their rings stay small on the
@@ -650,10 +927,9 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
       c.width = (double)a.grid.geom.width;
       c.per_query = qrad ? 1 : 0;
       c.ring_div = ring_div;
-      if (run_graph_passes<T>(a, c, dctl, sm, w.sm_count, s, ev[4], ev[5], &kernel_ms)) {
+      c.go = 1;
+      if (run_graph_passes<T>(w, a, c, dctl, sm, w.sm_count, s, ev[4], ev[5], &kernel_ms)) {
         const int passes = (int)c.iter - iter;
-        // the capture counted the search and step kernels once; each pass ran both
-        g_launches += 2ull * (unsigned long long)passes - 2ull;
         alg_bytes += (double)passes * n * d * sizeof(T) + (double)c.queries_run * d * sizeof(T) +
                      (double)c.accepted * K * (4.0 + sizeof(T));
         queries_run += c.queries_run;
@@ -672,8 +948,8 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     a.nq = nq;
     a.radius = r;
     a.fail_list = list[cur ^ 1];
-    KNNSJ_CUDA(cudaMemsetAsync(&sm->fail_count, 0, 4, s));
-    KNNSJ_CUDA(cudaMemsetAsync(&sm->fr, 0, sizeof(FailRadii), s));
+    launch_zero_words(&sm->fail_count, 4, s);
+    launch_zero_words(&sm->fr, sizeof(FailRadii), s);
     rec(4);
     launch_search<T>(a, w.sm_count, s);
     rec(5);
@@ -682,9 +958,8 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
       uint32_t pad;
       FailRadii fr;
     } tail;
-    KNNSJ_CUDA(cudaMemcpyAsync(&tail.fail, &sm->fail_count, 4, cudaMemcpyDeviceToHost, s));
-    if (qrad) KNNSJ_CUDA(cudaMemcpyAsync(&tail.fr, &sm->fr, sizeof(FailRadii), cudaMemcpyDeviceToHost, s));
-    KNNSJ_CUDA(cudaStreamSynchronize(s));
+    read_small(w, &tail.fail, &sm->fail_count, 4, s);
+    if (qrad) read_small(w, &tail.fr, &sm->fr, sizeof(FailRadii), s);
     const uint32_t nfail = tail.fail;
     const float pass_ms = elapsed(4, 5);
     kernel_ms += pass_ms;
@@ -717,9 +992,8 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   rec(2);
   unsigned long long cand = 0;
   uint32_t mlp_err = 0;
-  KNNSJ_CUDA(cudaMemcpyAsync(&cand, &sm->cand, 8, cudaMemcpyDeviceToHost, s));
-  if (qrad) KNNSJ_CUDA(cudaMemcpyAsync(&mlp_err, &sm->mlp_err, 4, cudaMemcpyDeviceToHost, s));
-  KNNSJ_CUDA(cudaStreamSynchronize(s));
+  read_small(w, &cand, &sm->cand, 8, s);
+  if (qrad) read_small(w, &mlp_err, &sm->mlp_err, 4, s);
   if (mlp_err)  // rows are still exact: the affected queries started at eps0
     fprintf(stderr, "knnsj: the tensor-core radius model timed out; those queries started at eps0\n");
   if (st) {
@@ -757,17 +1031,37 @@ double device_checksum(Workspace& w, const T* d_vals, uint64_t count, cudaStream
   SmallDev* sm = (SmallDev*)w.small.get(sizeof(SmallDev));
   launch_checksum<T>(d_vals, count, sm->cpart, &sm->csum, s);
   double v = 0.0;
-  KNNSJ_CUDA(cudaMemcpyAsync(&v, &sm->csum, sizeof(v), cudaMemcpyDeviceToHost, s));
-  KNNSJ_CUDA(cudaStreamSynchronize(s));
+  read_small(w, &v, &sm->csum, sizeof(v), s);
   return v;
 }
 template double device_checksum<float>(Workspace&, const float*, uint64_t, cudaStream_t);
 template double device_checksum<double>(Workspace&, const double*, uint64_t, cudaStream_t);
 
+// Streamed rows: waits (on s) for every block copy, then writes the rows
+// that passes after the first finished into the host buffers.  The caller
+// synchronises s.
+template <typename T>
+void finish_row_stream(Workspace& w, const RowStream& rows, const int32_t* d_ids, const T* d_dists, uint32_t K,
+                       cudaStream_t s) {
+  SmallDev* sm = (SmallDev*)w.small.p;
+  KNNSJ_CUDA(cudaEventRecord(w.chunk_ev[MAX_ROW_CHUNKS], w.copy_stream));
+  KNNSJ_CUDA(cudaStreamWaitEvent(s, w.chunk_ev[MAX_ROW_CHUNKS], 0));
+  patch_rows_kernel<T><<<(unsigned)(w.sm_count * 8), 256, 0, s>>>((const uint32_t*)w.chunk_list.p, &sm->patch_count,
+                                                                  d_ids, d_dists, K, (int32_t*)rows.ids_dev,
+                                                                  (T*)rows.d_dev);
+  KNNSJ_CHECK_LAUNCH();
+}
+
+template void finish_row_stream<float>(Workspace&, const RowStream&, const int32_t*, const float*, uint32_t,
+                                       cudaStream_t);
+template void finish_row_stream<double>(Workspace&, const RowStream&, const int32_t*, const double*, uint32_t,
+                                        cudaStream_t);
+
 template void run_join<float>(Workspace&, const JoinConfig&, const float*, const float*, uint64_t, uint32_t,
-                              uint32_t, int32_t*, float*, knnsj_stats*, cudaStream_t);
+                              uint32_t, int32_t*, float*, knnsj_stats*, cudaStream_t, RowStream*);
 template void run_join<double>(Workspace&, const JoinConfig&, const double*, const double*, uint64_t,
-                               uint32_t, uint32_t, int32_t*, double*, knnsj_stats*, cudaStream_t);
+                               uint32_t, uint32_t, int32_t*, double*, knnsj_stats*, cudaStream_t,
+                               RowStream*);
 template void run_features<float>(Workspace&, const JoinConfig&, const float*, const float*, uint64_t, uint32_t,
                                   uint32_t, float*, double*, cudaStream_t);
 template void run_features<double>(Workspace&, const JoinConfig&, const double*, const double*, uint64_t,

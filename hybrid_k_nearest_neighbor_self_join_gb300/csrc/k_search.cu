@@ -983,7 +983,7 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s) {
     const double e1 = std::sqrt((double)a.d) * (a.coord_bound * std::ldexp(1.0, -23) + std::ldexp(1.0, -140));
     p.filt_e1 = (float)(e1 * (1.0 + 1e-6));
   }
-  KNNSJ_CUDA(cudaMemsetAsync(a.work_counter, 0, sizeof(uint32_t), s));
+  launch_zero_words(a.work_counter, sizeof(uint32_t), s);
   const bool full = a.grid.geom.di == a.d;  // every dimension indexed
   switch (a.d) {
     case 2: full ? launch_one<T, 2, 2>(p, wpb, sm_count, s) : launch_one<T, 2, 0>(p, wpb, sm_count, s); break;

@@ -31,6 +31,8 @@ struct JoinConfig {
   int search_warps = 0;                    // search launch shape (0 = default), see SearchShape
   int search_qchunk = 0;
   int search_buffer = 0;
+  int row_chunks = 32;                     // host-pointer calls into pinned buffers: rows streamed out
+                                           // in this many blocks while the join runs (< 2: at the end)
 };
 
 // ReorderByDimension (main.cu:2521-2615).  `sample` holds rows 0, 100, 200,

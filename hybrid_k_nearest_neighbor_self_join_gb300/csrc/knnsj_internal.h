@@ -150,7 +150,7 @@ struct LoopCtl {
   unsigned long long queries_run;
   unsigned long long accepted;
   int per_query;       // per-query radii (learned starting radius)
-  int pad;
+  int go;              // the next pass runs (set by each pass's step)
   double ring_div;     // radii above width * ring_div / 2 force a rebuild (0: none)
   double redge[64];    // upper radius of each bin of the failing-radius histogram
 };
@@ -195,7 +195,26 @@ struct SearchLaunch {
 };
 template <typename T>
 void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s);
+// Clears bytes (a multiple of 4) with a kernel: unlike a runtime memset it
+// never waits behind copies in flight on another stream.
+void launch_zero_words(void* p, size_t bytes, cudaStream_t s);
 int search_buffer_capacity(uint32_t K);
+
+// Rows delivered to host buffers while the join runs (host-pointer calls
+// whose output buffers are pinned): the first pass runs in chunks of query
+// ids, each chunk's block of rows is copied out on a second stream as soon as
+// its search is done, and the rows that later passes finish are written into
+// the host buffers by a kernel at the end, after every chunk copy.
+constexpr int MAX_ROW_CHUNKS = 32;
+constexpr size_t MAIL_BYTES = 4096;  // mailbox: reads in the first half, writes in the second
+struct RowStream {
+  void* ids_host = nullptr;  // the host buffers
+  void* d_host = nullptr;
+  void* ids_dev = nullptr;   // their device-accessible addresses
+  void* d_dev = nullptr;
+  int chunks = 0;            // blocks of query ids in the first pass (>= 2)
+  bool active = false;       // set by run_join when it streamed
+};
 
 // ---- per-device workspace --------------------------------------------------
 struct Workspace {
@@ -206,12 +225,23 @@ struct Workspace {
   DevBuf keys0, keys1, vals0, vals1, hist, scan_tmp, flags, pos;  // grid build
   DevBuf ckeys, coff, dstart;            // cell tables
   DevBuf list0, list1, small, eps_partial, eps_sample, perm, minmax_part, qradius;
+  DevBuf chunk_list, patch_rows;         // streamed rows: queries by id block, rows finished late
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[8] = {};
+  cudaStream_t copy_stream = nullptr;    // streamed rows: device-to-host copies
+  cudaEvent_t chunk_ev[MAX_ROW_CHUNKS + 1] = {};
+  // While rows stream out, the copy engines are busy for tens of ms: the
+  // join's small reads and writes of host memory then go through the mailbox
+  // (mapped pinned memory that kernels read and write), device copies run on
+  // the SMs, and none of them queues behind the row copies.
+  void* mail_host = nullptr;
+  void* mail_dev = nullptr;
+  bool mail = false;
   int sm_count = 0;
   void* h_pinned = nullptr;
   size_t h_pinned_bytes = 0;
   void ensure_stream();
+  void ensure_copy_stream();  // and the mailbox
   void* pinned(size_t need);
   void pinned_release();
   void release_all();
@@ -224,7 +254,11 @@ struct JoinConfig;
 // is the same data on the host, used for the dimension-order sample.
 template <typename T>
 void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
-              uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s);
+              uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s,
+              RowStream* rows = nullptr);
+template <typename T>
+void finish_row_stream(Workspace& w, const RowStream& rows, const int32_t* d_ids, const T* d_dists, uint32_t K,
+                       cudaStream_t s);
 template <typename T>
 void run_features(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
                   uint32_t k, float* d_out, double* eps0_out, cudaStream_t s);

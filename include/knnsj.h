@@ -94,7 +94,8 @@ typedef struct {
   double ms_total;           /* device time of the whole join */
   double ms_prep;            /* reorder + transpose + epsilon + grid */
   double ms_search;          /* all search passes */
-  double ms_transfer;        /* host<->device copies (host-pointer calls) */
+  double ms_transfer;        /* host<->device copies (host-pointer calls; rows streamed into
+                                pinned buffers during the join count where they outlast it) */
   uint32_t perm[64];         /* dimension order used (first min(d,64)) */
   uint64_t kernel_launches;  /* CUDA kernels launched by the join */
   double ms_search_kernels;  /* device time of the search kernel launches only */
