@@ -42,11 +42,11 @@ constexpr uint32_t HIST_SPLIT = 4;  // blocks per histogram sample point
 #endif
 
 // One squared-distance term as the reference's double accumulator receives
-// it: a float product widened (no contraction across the type change) or a
-// double fma.
+// it: a float product widened (no contraction across the type change; the
+// widening is assembled from bits, off the FP64 pipe) or a double fma.
 __device__ __forceinline__ double eps_term(double acc, float a, float b) {
   const float df = __fsub_rn(a, b);
-  return __dadd_rn(acc, (double)__fmul_rn(df, df));
+  return __dadd_rn(acc, es_f2d(__fmul_rn(df, df)));
 }
 __device__ __forceinline__ double eps_term(double acc, double a, double b) {
   const double df = __dsub_rn(a, b);
@@ -57,7 +57,7 @@ __device__ __forceinline__ double eps_term(double acc, double a, double b) {
 // without the FP64 addition.
 __device__ __forceinline__ double eps_first(float a, float b) {
   const float df = __fsub_rn(a, b);
-  return (double)__fmul_rn(df, df);
+  return es_f2d(__fmul_rn(df, df));
 }
 __device__ __forceinline__ double eps_first(double a, double b) {
   const double df = __dsub_rn(a, b);
