@@ -72,27 +72,29 @@ __host__ __device__ __forceinline__ uint64_t terms_of_sample(uint64_t g, uint64_
 template <typename T>
 __global__ void eps_avg_chunk_kernel(const T* __restrict__ soa, uint64_t n, uint32_t d, uint64_t nthr,
                                      uint32_t nchunks, double* __restrict__ partial) {
+  // neighbouring lanes take neighbouring samples (the same chunk): their
+  // candidates t + 1000 m are neighbouring points, so each load is coalesced
   const uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= nthr * nchunks) return;
-  const uint64_t g = w / nchunks;
-  const uint32_t c = (uint32_t)(w % nchunks);
+  const uint64_t g = w % nthr;
+  const uint32_t c = (uint32_t)(w / nthr);
   const uint64_t tid = g * 1000;
   double s = 0.0;
   if (tid < n) {
     const uint64_t t = g % EPS_BLOCK;
     const uint64_t m_end = min(terms_of_sample(g, n), (uint64_t)(c + 1) * EPS_CHUNK);
+    // the sample point's first two coordinates stay in registers
+    const T q0 = soa[tid];
+    const T q1 = d > 1 ? soa[n + tid] : (T)0;
     // U terms at a time: their loads and square roots are independent; the
     // sum still runs term by term in ascending order
     constexpr int U = KNNSJ_EPS_UNROLL;
     for (uint64_t m = (uint64_t)c * EPS_CHUNK; m < m_end; m += U) {
       double rd[U];
-      {
-        const T q0 = soa[tid];
 #pragma unroll
-        for (int u = 0; u < U; u++) rd[u] = m + u < m_end ? eps_first(soa[t + 1000 * (m + u)], q0) : 0.0;
-      }
+      for (int u = 0; u < U; u++) rd[u] = m + u < m_end ? eps_first(soa[t + 1000 * (m + u)], q0) : 0.0;
       for (uint32_t l = 1; l < d; l++) {
-        const T ql = soa[(uint64_t)l * n + tid];
+        const T ql = l == 1 ? q1 : soa[(uint64_t)l * n + tid];
 #pragma unroll
         for (int u = 0; u < U; u++)
           if (m + u < m_end) rd[u] = eps_term(rd[u], soa[(uint64_t)l * n + t + 1000 * (m + u)], ql);
@@ -103,7 +105,7 @@ __global__ void eps_avg_chunk_kernel(const T* __restrict__ soa, uint64_t n, uint
         if (m + u < m_end) s = __dadd_rn(s, exact_sqrt(rd[u]));
     }
   }
-  partial[w] = s;
+  partial[g * nchunks + c] = s;
 }
 
 __global__ void eps_avg_sample_kernel(const double* __restrict__ partial, uint64_t nthr, uint32_t nchunks,
