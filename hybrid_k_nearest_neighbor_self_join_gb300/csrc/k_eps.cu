@@ -36,7 +36,10 @@ namespace {
 constexpr int EPS_BLOCK = 256;
 constexpr uint32_t NBUCKETS = 10000;
 constexpr uint32_t EPS_CHUNK = 256;
-constexpr uint32_t HIST_SPLIT = 4;  // blocks per histogram sample point
+#ifndef KNNSJ_HIST_SPLIT
+#define KNNSJ_HIST_SPLIT 16
+#endif
+constexpr uint32_t HIST_SPLIT = KNNSJ_HIST_SPLIT;  // blocks per histogram sample point
 #ifndef KNNSJ_EPS_UNROLL
 #define KNNSJ_EPS_UNROLL 4
 #endif
@@ -167,6 +170,13 @@ __global__ void __launch_bounds__(EPS_BLOCK) eps_hist_kernel(const T* __restrict
   const float errc = (float)(2 * d + 8) * 5.9604645e-8f;  // (2d+8) * 2^-24, relative
   const float abs_q = (float)(abs_err / bw) * 1.0001f + 1e-4f;
   const float flo = (float)b_lo, fhi = (float)b_hi;
+  // squared-distance prefilter: a pair whose float squared distance is at
+  // least s_hi has q32 - del >= fhi (the bracket below puts it above the
+  // counted range) -- q32 is within 2^-23 of sqrt(s32) / bw, and s_hi is
+  // widened by 2^-20 for its own rounding -- so it is skipped without a root
+  const double q_need = ((double)fhi + (double)abs_q) / (1.0 - (double)errc);
+  const double sq_bw = q_need * bw / ((1.0 - 1.0 / 8388608.0) * (1.0 - 1.0 / 8388608.0));
+  const float s_hi = __double2float_ru(sq_bw * sq_bw * (1.0 + 1.0 / 1048576.0));
   // the sample point's coordinates once per block; four candidates per
   // thread and round so that their loads overlap
   __shared__ T qs[MAX_D];
@@ -194,6 +204,7 @@ __global__ void __launch_bounds__(EPS_BLOCK) eps_hist_kernel(const T* __restrict
       const uint64_t p = i0 + u * STEP + threadIdx.x;
       if (p >= n || p == sid) continue;
       const float s32 = s4[u];
+      if (s32 >= s_hi) continue;
       const float q32 = __fmul_rn(__fsqrt_rn(s32), inv_bw);
       const float del = __fmaf_rn(errc, q32, abs_q);
       if (q32 - del >= 10000.5f) continue;  // certainly not below the mean
