@@ -52,6 +52,7 @@ knnsj_status make_config(const knnsj_options* o, uint32_t d, JoinConfig* c) {
   if (const char* e = env("KNNSJ_GRAPH")) c->use_graph = std::atoi(e);
   if (const char* e = env("KNNSJ_FLOAT_PREFILTER")) c->float_prefilter = std::atoi(e);
   if (const char* e = env("KNNSJ_ROW_CHUNKS")) c->row_chunks = std::atoi(e);
+  if (const char* e = env("KNNSJ_TAIL_BRUTE")) c->tail_brute = std::atoi(e);
   if (const char* e = env("KNNSJ_SEARCH_SHAPE")) {  // "warps,qchunk,buffer" (0 = default)
     int a = 0, b = 0, bb = 0;
     if (std::sscanf(e, "%d,%d,%d", &a, &b, &bb) >= 1) {

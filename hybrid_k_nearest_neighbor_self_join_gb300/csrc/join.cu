@@ -902,6 +902,23 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     // eps0 grid: no rebuild for the first pass
     const bool first_learned = qrad && iter == 0;
     if (!first_learned && regrid_due(rgrid, rmax, r_limit, (double)a.grid.geom.width, ring_div)) {
+      // sparse-query tail: a handful of queries (at most the work of about
+      // one rebuild, nq * n <= 2^32 distances) are finished exactly by a scan
+      // over all points instead of a coarser grid
+      if (cfg.tail_brute && nq <= 4096 && (uint64_t)nq * n <= (1ull << 32)) {
+        a.qlist = list[cur];
+        a.nq = nq;
+        rec(4);
+        launch_brute<T>(a, s);
+        rec(5);
+        KNNSJ_CUDA(cudaStreamSynchronize(s));
+        kernel_ms += elapsed(4, 5);
+        alg_bytes += (double)nq * n * d * sizeof(T) + (double)nq * K * (4.0 + sizeof(T));
+        queries_run += nq;
+        iter++;
+        nq = 0;
+        break;
+      }
       // coarser grid for the radius in flight (like main.cu:333-356); the
       // widened width keeps that radius's ring at three cells per dimension
       const T wnew = (T)(rgrid * (1.0 + 1.0 / 32768.0));

@@ -923,7 +923,107 @@ void launch_one(const SearchParams<T>& prm, int wpb_req, int sm_count, cudaStrea
   KNNSJ_CHECK_LAUNCH();
 }
 
+// Sparse-query tail: the exact K nearest points of each listed query by a
+// scan over every point (one CTA per query; its warps take equal shares of
+// the cell-ordered columns with the search kernel's selection, then warp 0
+// merges their selections and writes the row).  The distances use the search
+// kernel's arithmetic, so rows equal those of a ring search.
+constexpr int BRUTE_THREADS = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(BRUTE_THREADS) brute_kernel(const SearchParams<T> p) {
+  using Kt = Key<T>;
+  using KT = typename Kt::type;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t s_len[BRUTE_THREADS / 32];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  const uint32_t B = p.B, K = p.K;
+  const uint64_t n = p.n;
+  KT* bufs = reinterpret_cast<KT*>(smem);
+  KT* buf = bufs + (size_t)wib * B;
+  uint32_t* hist = reinterpret_cast<uint32_t*>(bufs + (size_t)wpb * B) + wib * 256;
+  T* qs = reinterpret_cast<T*>(reinterpret_cast<uint32_t*>(bufs + (size_t)wpb * B) + wpb * 256);
+  const uint32_t qid = p.qlist[blockIdx.x];
+  for (uint32_t l = threadIdx.x; l < p.d; l += blockDim.x) qs[l] = p.xs[(uint64_t)l * n + qid];
+  __syncthreads();
+  Sel<T> st;
+  st.len = 0;
+  st.tau = Kt::bound((T)INFINITY);
+  st.tight = false;
+  const uint64_t share = (n + wpb - 1) / wpb;
+  const uint64_t j0 = (uint64_t)wib * share;
+  const uint64_t j1 = min(n, j0 + share);
+  for (uint64_t v0 = j0; v0 < j1; v0 += 32) {
+    const uint64_t j = v0 + lane;
+    bool pass = false;
+    KT key = Kt::maxv();
+    if (j < j1) {
+      T acc = 0;
+      for (uint32_t l = 0; l < p.d; l++) {
+        const T t = Num<T>::sub(p.ps[(uint64_t)l * n + j], qs[l]);
+        acc = Num<T>::fma(t, t, acc);
+      }
+      key = Kt::make(acc, p.pid[j]);
+      pass = Kt::less(key, st.tau);
+    }
+    const unsigned m = __ballot_sync(FULL, pass);
+    if (m) {
+      if (pass) buf[st.len + __popc(m & lanemask_lt())] = key;
+      st.len += __popc(m);
+      if (st.len > B - 32) st = reduce<T>(buf, hist, st, K, B, lane);
+    }
+  }
+  if (lane == 0) s_len[wib] = st.len;
+  __syncthreads();
+  if (wib != 0) return;
+  for (int w = 1; w < wpb; w++) {
+    const KT* ob = bufs + (size_t)w * B;
+    const uint32_t lw = s_len[w];
+    for (uint32_t b0 = 0; b0 < lw; b0 += 32) {
+      bool pass = false;
+      KT key = Kt::maxv();
+      if (b0 + lane < lw) {
+        key = ob[b0 + lane];
+        pass = Kt::less(key, st.tau);
+      }
+      const unsigned m = __ballot_sync(FULL, pass);
+      if (m) {
+        if (pass) buf[st.len + __popc(m & lanemask_lt())] = key;
+        st.len += __popc(m);
+        if (st.len > B - 32) st = reduce<T>(buf, hist, st, K, B, lane);
+      }
+    }
+  }
+  write_sorted_row_bitonic<T>(buf, st.len, K, p.out_ids, p.out_d, (uint64_t)qid * K, lane);
+}
+
 }  // namespace
+
+template <typename T>
+void launch_brute(const SearchLaunch<T>& a, cudaStream_t s) {
+  if (a.nq == 0) return;
+  SearchParams<T> p{};
+  p.ps = a.grid.ps;
+  p.xs = a.xs;
+  p.pid = a.grid.pid;
+  p.n = a.n;
+  p.d = a.d;
+  p.K = a.K;
+  p.B = (uint32_t)search_buffer_capacity(a.K);
+  p.qlist = a.qlist;
+  p.nq = a.nq;
+  p.out_ids = a.out_ids;
+  p.out_d = a.out_d;
+  const size_t per_warp = (size_t)p.B * sizeof(typename Key<T>::type) + 256 * 4;
+  int wpb = BRUTE_THREADS / 32;
+  while (wpb > 1 && per_warp * wpb + a.d * sizeof(T) > 200 * 1024) wpb--;
+  const size_t smem = per_warp * wpb + a.d * sizeof(T);
+  KNNSJ_CUDA(cudaFuncSetAttribute(brute_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  brute_kernel<T><<<a.nq, wpb * 32, smem, s>>>(p);
+  KNNSJ_CHECK_LAUNCH();
+}
 
 // Selection buffer per warp: room for K keys plus a full chunk of 32, and at
 // least HIST_MAX_B so the histogram reduce runs rarely.
@@ -999,5 +1099,7 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s) {
 
 template void launch_search<float>(const SearchLaunch<float>&, int, cudaStream_t);
 template void launch_search<double>(const SearchLaunch<double>&, int, cudaStream_t);
+template void launch_brute<float>(const SearchLaunch<float>&, cudaStream_t);
+template void launch_brute<double>(const SearchLaunch<double>&, cudaStream_t);
 
 }  // namespace knnsj

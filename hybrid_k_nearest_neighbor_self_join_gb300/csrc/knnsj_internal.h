@@ -199,6 +199,9 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s);
 // never waits behind copies in flight on another stream.
 void launch_zero_words(void* p, size_t bytes, cudaStream_t s);
 int search_buffer_capacity(uint32_t K);
+// Exact rows of the queries a.qlist[0..a.nq) by a scan over all points.
+template <typename T>
+void launch_brute(const SearchLaunch<T>& a, cudaStream_t s);
 
 // Rows delivered to host buffers while the join runs (host-pointer calls
 // whose output buffers are pinned): the first pass runs in chunks of query

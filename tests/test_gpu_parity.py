@@ -147,20 +147,43 @@ def test_graph_passes_match_host_passes(monkeypatch, mode):
         assert a_s[key] == b_s[key], key
 
 
-def test_far_outliers_rebuild_for_the_widest_ring():
+@pytest.mark.parametrize("tail", ["0", "1"])
+def test_far_outliers(monkeypatch, tail):
     # a tight 6-D cluster and a few far outliers: the outliers' radii grow
-    # far past the cluster's, so the grid is rebuilt for the largest radius
-    # (rings stay within the row cap); rows still match brute force
+    # far past the cluster's.  Tail "0": the grid is rebuilt for the largest
+    # radius (rings stay within the row cap); tail "1": the last few queries
+    # are finished by an exact scan over all points.  Rows match brute force.
+    monkeypatch.setenv("KNNSJ_TAIL_BRUTE", tail)
     rng = np.random.default_rng(23)
     c = rng.normal(0.0, 0.01, (40_000, 6)).astype(np.float32)
     o = rng.uniform(-1.0, 1.0, (12, 6)).astype(np.float32)
     x = np.concatenate([c, o])
     ids, dists, st = kj.selfjoin(x, 16, beta=0.05, radius_mode=kj.RADIUS_LEARNED, return_stats=True)
-    assert st["regrids"] >= 1
+    if tail == "0":
+        assert st["regrids"] >= 1
     perm, _ = kj.reorder_dims(x)
     q = np.concatenate([np.arange(40_000, 40_012), np.arange(0, 40_000, 997)])
     bi, bd = oracle.bruteforce(x[:, perm], 17, q)
     assert_same(ids[q], dists[q], bi, bd)
+
+
+@pytest.mark.parametrize("dtype,mode", [(np.float32, kj.RADIUS_PLAIN), (np.float64, kj.RADIUS_LEARNED)])
+def test_sparse_tail_matches_ring_search(monkeypatch, dtype, mode):
+    # 2-D clumps with a few isolated points: the same rows whether the last
+    # queries are finished by the exact scan or by rebuilt grids
+    rng = np.random.default_rng(24)
+    c = (rng.normal(0.0, 0.002, (60_000, 2)) + rng.integers(0, 4, (60_000, 1)) * 0.01).astype(dtype)
+    o = rng.uniform(-1.0, 1.0, (7, 2)).astype(dtype)
+    x = np.concatenate([c, o])
+    out = {}
+    for tail in ("0", "1"):
+        monkeypatch.setenv("KNNSJ_TAIL_BRUTE", tail)
+        out[tail] = kj.selfjoin(x, 24, beta=0.0, radius_mode=mode)
+    assert np.array_equal(out["0"][0], out["1"][0]) and np.array_equal(out["0"][1], out["1"][1])
+    perm, _ = kj.reorder_dims(x)
+    q = np.arange(60_000, 60_007)
+    bi, bd = oracle.bruteforce(x[:, perm], 25, q)
+    assert_same(out["1"][0][q], out["1"][1][q], bi, bd)
 
 
 def test_tiny_input_eps_fallback():
