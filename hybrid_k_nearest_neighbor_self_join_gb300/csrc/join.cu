@@ -902,10 +902,13 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     // eps0 grid: no rebuild for the first pass
     const bool first_learned = qrad && iter == 0;
     if (!first_learned && regrid_due(rgrid, rmax, r_limit, (double)a.grid.geom.width, ring_div)) {
-      // sparse-query tail: a handful of queries (at most the work of about
-      // one rebuild, nq * n <= 2^32 distances) are finished exactly by a scan
-      // over all points instead of a coarser grid
-      if (cfg.tail_brute && nq <= 4096 && (uint64_t)nq * n <= (1ull << 32)) {
+      // sparse-query tail: when the largest radius has outgrown the grid
+      // (its ring would pass the row cap) and only a handful of queries are
+      // left (nq * n <= 2^32 distances), they are finished exactly by a scan
+      // over all points instead of a grid coarse enough for that radius
+      // (tail_brute 2, for tests: at any due rebuild)
+      const bool outgrown = ring_too_wide(rmax, (double)a.grid.geom.width, ring_div) || cfg.tail_brute == 2;
+      if (cfg.tail_brute && outgrown && nq <= 4096 && (uint64_t)nq * n <= (1ull << 32)) {
         a.qlist = list[cur];
         a.nq = nq;
         rec(4);

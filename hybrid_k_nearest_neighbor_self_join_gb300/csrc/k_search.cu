@@ -201,6 +201,18 @@ __device__ __forceinline__ void sort_reduce(typename Key<T>::type* buf, Sel<T>& 
   __syncwarp();
 }
 
+// Monotone bin of a squared distance, round(a * scale) clamped to top, on
+// the FMA pipe (a float-to-int conversion runs on a narrower pipe): with
+// 1.5 * 2^23 added, the integer lands in the low mantissa bits.  Both users
+// only need a monotone map that sends the largest kept key to a bin <= top.
+__device__ __forceinline__ int acc_bin(float a, float scale, int top) {
+  return min(__float_as_int(__fmaf_rn(a, scale, 12582912.0f)) - 0x4b400000, top);
+}
+// scale that maps [0, tacc] onto [0, nb] (0 when tacc is 0 or huge)
+__device__ __forceinline__ float bin_scale(float nb, float tacc) {
+  return (tacc > 0.0f && tacc < 3.0e38f) ? __fdividef(nb, tacc) : 0.0f;
+}
+
 // Keeps the keys of the lowest histogram bins that hold at least K keys
 // (bins split [0, acc(tau)] evenly); the new threshold is the largest kept
 // key.  Needs st.len >= K and B <= HIST_MAX_B.
@@ -211,12 +223,12 @@ __device__ void hist_reduce(typename Key<T>::type* buf, uint32_t* hist, Sel<T>& 
   using KT = typename Kt::type;
   // bins by a monotone float map of the distance: equal distances share a bin
   const float tacc = to_float_up(Kt::acc(st.tau));
-  const float scale = tacc > 0.0f ? 32.0f / tacc : 0.0f;
+  const float scale = bin_scale(32.0f, tacc);
   __syncwarp();
   hist[lane] = 0;
   __syncwarp();
   for (uint32_t i = lane; i < st.len; i += 32) {
-    const int b = min((int)((float)Kt::acc(buf[i]) * scale), 31);
+    const int b = acc_bin((float)Kt::acc(buf[i]), scale, 31);
     atomicAdd(&hist[b], 1u);
   }
   __syncwarp();
@@ -244,7 +256,7 @@ __device__ void hist_reduce(typename Key<T>::type* buf, uint32_t* hist, Sel<T>& 
     const uint32_t i = base + lane;
     KT v = Kt::maxv();
     if (i < st.len) v = buf[i];
-    const bool keep = i < st.len && min((int)((float)Kt::acc(v) * scale), 31) <= bst;
+    const bool keep = i < st.len && acc_bin((float)Kt::acc(v), scale, 31) <= bst;
     const unsigned m = __ballot_sync(FULL, keep);
     __syncwarp();
     if (keep) {
@@ -306,10 +318,10 @@ __device__ KNNSJ_WRITE_LINKAGE void write_sorted_row(typename Key<T>::type* buf,
   using KT = typename Kt::type;
   constexpr int R = HIST_MAX_B / 32;
   const float tacc = to_float_up(Kt::acc(top));
-  const float scale = tacc > 0.0f ? 256.0f / tacc : 0.0f;
+  const float scale = bin_scale(256.0f, tacc);
   __syncwarp();
-#pragma unroll
-  for (int r = 0; r < 8; r++) cnt[r * 32 + lane] = 0;
+  reinterpret_cast<uint4*>(cnt)[lane] = make_uint4(0u, 0u, 0u, 0u);
+  reinterpret_cast<uint4*>(cnt)[lane + 32] = make_uint4(0u, 0u, 0u, 0u);
   __syncwarp();
   KT v[R];
   uint32_t slot[R];
@@ -320,18 +332,21 @@ __device__ KNNSJ_WRITE_LINKAGE void write_sorted_row(typename Key<T>::type* buf,
     slot[r] = 0;
     if (r * 32 < (int)len && i < len) {
       v[r] = buf[i];
-      const int b = min((int)((float)Kt::acc(v[r]) * scale), 255);
+      const int b = acc_bin((float)Kt::acc(v[r]), scale, 255);
       slot[r] = atomicAdd(&cnt[b], 1u);
     }
   }
   __syncwarp();
   // exclusive scan of the 256 bin counts, 8 consecutive bins per lane
   uint32_t c[8], s = 0;
-#pragma unroll
-  for (int t = 0; t < 8; t++) {
-    c[t] = cnt[lane * 8 + t];
-    s += c[t];
+  {
+    const uint4 c0 = reinterpret_cast<const uint4*>(cnt)[lane * 2];
+    const uint4 c1 = reinterpret_cast<const uint4*>(cnt)[lane * 2 + 1];
+    c[0] = c0.x, c[1] = c0.y, c[2] = c0.z, c[3] = c0.w;
+    c[4] = c1.x, c[5] = c1.y, c[6] = c1.z, c[7] = c1.w;
   }
+#pragma unroll
+  for (int t = 0; t < 8; t++) s += c[t];
   uint32_t incl = s;
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
@@ -340,10 +355,15 @@ __device__ KNNSJ_WRITE_LINKAGE void write_sorted_row(typename Key<T>::type* buf,
   }
   uint32_t run = incl - s;
   __syncwarp();
+  {
+    uint32_t o[8];
 #pragma unroll
-  for (int t = 0; t < 8; t++) {
-    cnt[lane * 8 + t] = run;
-    run += c[t];
+    for (int t = 0; t < 8; t++) {
+      o[t] = run;
+      run += c[t];
+    }
+    reinterpret_cast<uint4*>(cnt)[lane * 2] = make_uint4(o[0], o[1], o[2], o[3]);
+    reinterpret_cast<uint4*>(cnt)[lane * 2 + 1] = make_uint4(o[4], o[5], o[6], o[7]);
   }
   __syncwarp();
   // scatter by bin (order inside a bin still arbitrary)
@@ -353,7 +373,7 @@ __device__ KNNSJ_WRITE_LINKAGE void write_sorted_row(typename Key<T>::type* buf,
     const uint32_t i = r * 32 + lane;
     pos[r] = 0xffffffffu;
     if (r * 32 < (int)len && i < len) {
-      const int b = min((int)((float)Kt::acc(v[r]) * scale), 255);
+      const int b = acc_bin((float)Kt::acc(v[r]), scale, 255);
       pos[r] = cnt[b] + slot[r];
       buf[pos[r]] = v[r];
     }
@@ -380,7 +400,7 @@ __device__ KNNSJ_WRITE_LINKAGE void write_sorted_row(typename Key<T>::type* buf,
     const uint32_t pp = p0 + lane;
     if (pp < end) {
       const KT w = buf[pp];
-      const int b = min((int)((float)Kt::acc(w) * scale), 255);
+      const int b = acc_bin((float)Kt::acc(w), scale, 255);
       const uint32_t first = cnt[b];
       const uint32_t last = b < 255 ? cnt[b + 1] : len;
       uint32_t rank = 0;
@@ -928,7 +948,7 @@ void launch_one(const SearchParams<T>& prm, int wpb_req, int sm_count, cudaStrea
 // the cell-ordered columns with the search kernel's selection, then warp 0
 // merges their selections and writes the row).  The distances use the search
 // kernel's arithmetic, so rows equal those of a ring search.
-constexpr int BRUTE_THREADS = 256;
+constexpr int BRUTE_THREADS = 1024;
 
 template <typename T>
 __global__ void __launch_bounds__(BRUTE_THREADS) brute_kernel(const SearchParams<T> p) {

@@ -31,8 +31,8 @@ struct JoinConfig {
   int search_warps = 0;                    // search launch shape (0 = default), see SearchShape
   int search_qchunk = 0;
   int search_buffer = 0;
-  int tail_brute = 1;                      // a few queries that would force a grid rebuild are finished
-                                           // by an exact scan over all points instead
+  int tail_brute = 1;                      // a few queries whose radius outgrew the grid are finished by
+                                           // an exact scan over all points (2: at any due rebuild; 0: off)
   int row_chunks = 32;                     // host-pointer calls into pinned buffers: rows streamed out
                                            // in this many blocks while the join runs (< 2: at the end)
 };
