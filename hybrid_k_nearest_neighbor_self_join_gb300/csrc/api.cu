@@ -179,6 +179,7 @@ void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t 
       rs.ids_dev = ai.devicePointer;
       rs.d_dev = ad.devicePointer;
       rs.chunks = cfg.row_chunks;
+      rs.checksum = st && checksum;
       rsp = &rs;
     }
     cudaGetLastError();  // an unregistered pointer is not an error here
@@ -193,25 +194,23 @@ void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t 
   } copy_wait;
   if (rsp) copy_wait.w = &w;
   run_join<T>(w, cfg, din, data, n, d, k, dids, ddist, st, s, rsp);
-  // (the checksum runs while the last row copies are still in flight)
-  if (st && checksum) st->total_distance = device_checksum<T>(w, ddist, n * K, s);
+  const bool streamed = rsp && rsp->active;  // rows already in place, checksum taken
+  if (st && checksum) st->total_distance = streamed ? rsp->total_distance : device_checksum<T>(w, ddist, n * K, s);
   cudaEvent_t t2, t3;
   KNNSJ_CUDA(cudaEventCreate(&t2));
   KNNSJ_CUDA(cudaEventCreate(&t3));
   KNNSJ_CUDA(cudaEventRecord(t2, s));
-  if (rsp && rsp->active) {
-    finish_row_stream<T>(w, *rsp, dids, ddist, (uint32_t)K, s);
-  } else {
+  if (!streamed) {
     KNNSJ_CUDA(cudaMemcpyAsync(out_ids, dids, n * K * 4, cudaMemcpyDeviceToHost, s));
     KNNSJ_CUDA(cudaMemcpyAsync(out_d, ddist, n * K * sizeof(T), cudaMemcpyDeviceToHost, s));
   }
   KNNSJ_CUDA(cudaEventRecord(t3, s));
   KNNSJ_CUDA(cudaStreamSynchronize(s));
-  if (st) {  // streamed rows: the copies that outlast the join
+  if (st) {  // (streamed rows: run_join counted the copies that outlast the join)
     float a = 0, b = 0;
     cudaEventElapsedTime(&a, t0, t1);
     cudaEventElapsedTime(&b, t2, t3);
-    st->ms_transfer = a + b;
+    st->ms_transfer = a + (streamed ? st->ms_transfer : b);
   }
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);

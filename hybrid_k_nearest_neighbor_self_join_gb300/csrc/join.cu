@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <vector>
 
@@ -627,7 +628,8 @@ static double decode_radius(unsigned long long bits) {
 template <typename T>
 static bool run_graph_passes(Workspace& w, SearchLaunch<T> a, LoopCtl& c, LoopCtl* dctl, SmallDev* sm,
                              int sm_count, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1, double* kernel_ms,
-                             bool upload = true, uint32_t iter_before = 0) {
+                             bool upload = true, uint32_t iter_before = 0,
+                             const std::function<void()>& after_launch = {}) {
   // launches are counted as they ran: the body's once per pass, the
   // condition node once
   if (upload) iter_before = c.iter;
@@ -697,6 +699,7 @@ static bool run_graph_passes(Workspace& w, SearchLaunch<T> a, LoopCtl& c, LoopCt
     KNNSJ_CUDA(cudaEventRecord(e0, s));
     KNNSJ_CUDA(cudaGraphLaunch(ex, s));
     KNNSJ_CUDA(cudaEventRecord(e1, s));
+    if (after_launch) after_launch();  // device work that can precede the host's look at the state
     read_small(w, &c, dctl, sizeof(LoopCtl), s);
     const unsigned long long passes = c.iter - iter_before;
     g_launches = g_launches - body + body * passes + 1;
@@ -791,6 +794,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   // (the caller waits for the copies and patches the late rows in:
   // finish_row_stream)
   const bool streamed = rows && rows->chunks >= 2 && n >= (uint64_t)rows->chunks;
+  bool checksum_done = false;  // streamed rows: the checksum of the final table is launched
   if (streamed) {
     w.ensure_copy_stream();
     w.mail = true;
@@ -851,7 +855,17 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     if (dev_loop) {
       loop_step_kernel<T><<<1, 1, 0, s>>>(dctl, &sm->fail_count, &sm->fr, 0, 0);
       KNNSJ_CHECK_LAUNCH();
-      ran = run_graph_passes<T>(w, a, c, dctl, sm, w.sm_count, s, ev[4], ev[5], &kernel_ms, false, 1);
+      // the result checksum goes right behind the graph: if the graph
+      // finishes the join, it overlaps the row copies (the host's read of the
+      // loop state waits behind them)
+      auto early_checksum = [&]() {
+        if (rows->checksum) {
+          launch_checksum<T>(d_dists, n * K, sm->cpart, &sm->csum, s);
+          checksum_done = true;
+        }
+      };
+      ran = run_graph_passes<T>(w, a, c, dctl, sm, w.sm_count, s, ev[4], ev[5], &kernel_ms, false, 1,
+                                early_checksum);
       if (ran) {
         const int passes = (int)c.iter - 1;
         alg_bytes += (double)passes * n * d * sizeof(T);
@@ -897,6 +911,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   }
 
   while (nq > 0) {
+    checksum_done = false;  // more passes change the table
     if (iter >= max_iter) throw StatusError{KNNSJ_ERR_NO_CONVERGENCE, "iteration cap reached"};
     // learned starting radii are clamped so their rings stay small on the
     // eps0 grid: no rebuild for the first pass
@@ -1010,6 +1025,16 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     }
   }
   rec(2);
+  if (streamed) {
+    // the result checksum runs while the last row copies are in flight; the
+    // wait for them and the late rows follow, and the small reads below come
+    // after the copies instead of queueing behind them
+    if (rows->checksum && !checksum_done) launch_checksum<T>(d_dists, n * K, sm->cpart, &sm->csum, s);
+    finish_row_stream<T>(w, *rows, d_ids, d_dists, K, s);
+    rec(3);
+    w.mail = false;
+    if (rows->checksum) read_small(w, &rows->total_distance, &sm->csum, sizeof(double), s);
+  }
   unsigned long long cand = 0;
   uint32_t mlp_err = 0;
   read_small(w, &cand, &sm->cand, 8, s);
@@ -1030,6 +1055,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     st->ms_prep = a01;
     st->ms_search = a12;
     st->ms_total = a01 + a12;
+    if (streamed) st->ms_transfer = elapsed(2, 3);  // the row copies that outlast the join
   }
 }
 

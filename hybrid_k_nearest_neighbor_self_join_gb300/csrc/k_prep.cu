@@ -9,6 +9,7 @@
 
 #include <cfloat>
 
+#include "exact_sqrt.cuh"
 #include "knnsj_internal.h"
 
 namespace knnsj {
@@ -90,6 +91,10 @@ constexpr unsigned CHECKSUM_BLOCKS = 1024;
 // Squared distance in DTYPE, widened and added in double (GPU.cu:3690-3693);
 // fixed grid, fixed per-thread order and a fixed tree, so the figure is the
 // same on every run.
+// exact widening to double (float: assembled from bits, off the FP64 pipe)
+__device__ __forceinline__ double widen(float x) { return es_f2d(x); }
+__device__ __forceinline__ double widen(double x) { return x; }
+
 template <typename T>
 __global__ void checksum_kernel(const T* __restrict__ v, uint64_t count, double* __restrict__ part) {
   __shared__ double ws[32];
@@ -97,7 +102,7 @@ __global__ void checksum_kernel(const T* __restrict__ v, uint64_t count, double*
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const T x = v[i];
-    s = __dadd_rn(s, (double)Num<T>::mul(x, x));
+    s = __dadd_rn(s, widen(Num<T>::mul(x, x)));
   }
   for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(FULL, s, off);
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;

@@ -216,7 +216,9 @@ struct RowStream {
   void* ids_dev = nullptr;   // their device-accessible addresses
   void* d_dev = nullptr;
   int chunks = 0;            // blocks of query ids in the first pass (>= 2)
-  bool active = false;       // set by run_join when it streamed
+  bool checksum = false;     // also compute the result's verification sum
+  bool active = false;       // set by run_join when it streamed (rows complete on return)
+  double total_distance = 0.0;
 };
 
 // ---- per-device workspace --------------------------------------------------
