@@ -621,6 +621,19 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
         return lbf * (1.0f - 1.0f / 16384.0f);
       };
 
+      // The dimension-0 cells [xl, xh] of a row with lower bound lbs that can
+      // hold a point whose computed squared distance is <= tupv (float,
+      // rounded up); false when none can.
+      auto cut_row = [&](float lbs, float tupv, uint32_t& xl, uint32_t& xh) -> bool {
+        if (lbs > tupv) return false;
+        const float avail = tupv * (1.0f + 1.0f / 16384.0f) - lbs;
+        const float g = sqrtf(fmaxf(avail, 0.0f)) * (1.0f + 1.0f / 1048576.0f);
+        const float slack = (fabsf(qf[0]) + g) * (1.0f / 2097152.0f);
+        xl = max(xl, ring_cell(qf[0] - g - slack, s_minf[0], s_invw, p.g.ncell[0], false));
+        xh = min(xh, ring_cell(qf[0] + g + slack, s_minf[0], s_invw, p.g.ncell[0], true));
+        return xl <= xh;
+      };
+
       Sel<T> st;
       st.len = 0;
       st.tau = Kt::bound(thr);
@@ -676,7 +689,14 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
           rs = re = 0;
           if (ridx < nrows) {
             rlb = row_info((uint32_t)ridx, rbase);
-            run_of(p, rbase + lo[0], rbase + hi[0], rs, re);
+            // three or more indexed dimensions: only the row's dimension-0
+            // interval that can hold a point under the current threshold (the
+            // radius, until K keys are held) -- the corners of a cube of
+            // cells hold most of its points; with two, rows are cut only once
+            // K keys are held (measured: the cut costs more than it saves)
+            uint32_t xl = lo[0], xh = hi[0];
+            const bool cut = DI >= 3 || (DI == 0 && di >= 3);
+            if (!cut || cut_row(rlb, to_float_up(Kt::acc(st.tau)), xl, xh)) run_of(p, rbase + xl, rbase + xh, rs, re);
           }
           if (KNNSJ_EARLY_FAIL && nrows <= 32) {
             uint32_t cnt = re - rs;
@@ -713,22 +733,9 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
         uint32_t sA = 0, eA = 0;
         if (active) {
           uint32_t xl = lo[0], xh = hi[0];
-          bool empty = false;
-          if (have) {
-            if (lbs > tup) {
-              empty = true;
-            } else {
-              // dimension-0 interval that can still hold a better point
-              const float avail = tup * (1.0f + 1.0f / 16384.0f) - lbs;
-              const float g = sqrtf(fmaxf(avail, 0.0f)) * (1.0f + 1.0f / 1048576.0f);
-              const float slack = (fabsf(qf[0]) + g) * (1.0f / 2097152.0f);
-              const uint32_t a0 = ring_cell(qf[0] - g - slack, s_minf[0], s_invw, p.g.ncell[0], false);
-              const uint32_t b0 = ring_cell(qf[0] + g + slack, s_minf[0], s_invw, p.g.ncell[0], true);
-              xl = max(xl, a0);
-              xh = min(xh, b0);
-              empty = xl > xh;
-            }
-          }
+          // (the group's run already holds the row cut to the threshold of
+          // its loading; with K keys held the row is cut again)
+          const bool empty = have && !cut_row(lbs, tup, xl, xh);
           if (!empty) {
             if (xl == lo[0] && xh == hi[0]) {
               sA = s0;
