@@ -201,6 +201,19 @@ __device__ __forceinline__ void sort_reduce(typename Key<T>::type* buf, Sel<T>& 
   __syncwarp();
 }
 
+// Row-index divisors of small ring extents: 0xffffffff / e + 1 (0 for e <= 1),
+// read from the constant cache instead of divided per query.
+constexpr uint32_t MAGIC_TAB = 64;
+struct MagicTable {
+  uint32_t v[MAGIC_TAB + 1];
+};
+constexpr MagicTable make_magic_table() {
+  MagicTable t{};
+  for (uint32_t e = 0; e <= MAGIC_TAB; e++) t.v[e] = e > 1 ? 0xffffffffu / e + 1u : 0u;
+  return t;
+}
+__constant__ MagicTable c_magic = make_magic_table();
+
 // Monotone bin of a squared distance, round(a * scale) clamped to top, on
 // the FMA pipe (a float-to-int conversion runs on a narrower pipe): with
 // 1.5 * 2^23 added, the integer lands in the low mantissa bits.  Both users
@@ -577,7 +590,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
           hi[j] = ring_cell(qf[j] + rf + slack, s_minf[j], s_invw, p.g.ncell[j], true);
           const uint32_t ext = hi[j] - lo[j] + 1;
           // x / ext == umulhi(x, magic) for small x; rows are indexed by dims 1..
-          if (j > 0) magic[j] = ext > 1 ? 0xffffffffu / ext + 1u : 0u;
+          if (j > 0) magic[j] = ext <= MAGIC_TAB ? c_magic.v[ext] : 0xffffffffu / ext + 1u;
         }
       }
       unsigned long long nrows = 1;
