@@ -140,8 +140,12 @@ __host__ __device__ inline int32_t es_f2i_rn(float f) {
 // conversion instruction runs on the FP64 pipe of this GPU.
 __host__ __device__ inline double es_f2d(float f) {
   const uint32_t b = es_bits_of_float(f);
-  const uint64_t sign = (uint64_t)(b >> 31) << 63;
   const uint32_t ef = (b >> 23) & 0xffu;
+  // normal floats: rebias the exponent (by 896, in place) and widen the
+  // significand -- one 64-bit shift and an add
+  if (ef - 1u < 254u)
+    return es_from_bits((((uint64_t)(b & 0x7fffffffu)) << 29) + (896ull << 52) + ((uint64_t)(b >> 31) << 63));
+  const uint64_t sign = (uint64_t)(b >> 31) << 63;
   uint32_t mf = b & 0x7fffffu;
   if (ef == 0xffu) return es_from_bits(sign | (0x7ffull << 52) | ((uint64_t)mf << 29));  // inf, nan
   if (ef == 0) {
