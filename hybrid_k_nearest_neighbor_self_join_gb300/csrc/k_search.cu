@@ -417,7 +417,8 @@ __device__ KNNSJ_WRITE_LINKAGE void write_sorted_row(typename Key<T>::type* buf,
       const uint32_t first = cnt[b];
       const uint32_t last = b < 255 ? cnt[b + 1] : len;
       uint32_t rank = 0;
-      for (uint32_t j = first; j < last; j++) rank += Kt::less(buf[j], w) ? 1u : 0u;
+      if (last - first > 1)  // a key alone in its bin is ranked by the bin
+        for (uint32_t j = first; j < last; j++) rank += Kt::less(buf[j], w) ? 1u : 0u;
       const uint32_t fin = first + rank;
       if (fin < K) {
         out_ids[row_out + fin] = (int32_t)Kt::id(w);
