@@ -259,22 +259,27 @@ def run_gb300(args):
     xs_np, ids_np, d_np = hx.numpy(), hids.numpy(), hd.numpy()
 
     def host_step():
-        kj.selfjoin(xs_np, k, num_indexed_dims=di, beta=beta, radius_mode=kj.RADIUS_LEARNED, out_ids=ids_np,
-                    out_dists=d_np)
+        return kj.selfjoin(xs_np, k, num_indexed_dims=di, beta=beta, radius_mode=kj.RADIUS_LEARNED,
+                           out_ids=ids_np, out_dists=d_np, return_stats=True)[2]
 
     host_step()
     torch.cuda.synchronize()
     dist.barrier()
-    e2 = torch.cuda.Event(enable_timing=True)
-    e3 = torch.cuda.Event(enable_timing=True)
-    e2.record()
     e2e_steps = max(1, min(args.steps, 3))
-    for _ in range(e2e_steps):
-        host_step()
-    e3.record()
+    marks = [torch.cuda.Event(enable_timing=True) for _ in range(e2e_steps + 1)]
+    marks[0].record()
+    e2e_stats = []
+    for i in range(e2e_steps):
+        e2e_stats.append(host_step())
+        marks[i + 1].record()
     torch.cuda.synchronize()
-    t_e2e = dist.max(e2.elapsed_time(e3))
+    t_e2e = dist.max(marks[0].elapsed_time(marks[-1]))
     e2e_value = n * world * e2e_steps / (t_e2e / 1e3)
+    e2e_ms_steps = [round(marks[i].elapsed_time(marks[i + 1]), 2) for i in range(e2e_steps)]
+    # rows were streamed to the host during the join when the copies that
+    # outlast it are short (one copy of the 13 GB table after the join takes
+    # tens of ms)
+    e2e_streamed = all(s_["ms_transfer"] < 0.5 * s_["ms_search"] for s_ in e2e_stats)
 
     # ---- roofline of the dominant kernel (the search) ----------------------
     pk = peaks()
@@ -304,7 +309,8 @@ def run_gb300(args):
                    "radius": "learned starting radius (built-in model)", "parallelism": f"replicas x{world}",
                    "l2": "inputs (200 MB) and outputs (13 GB) exceed the 129 MB L2; no flush"},
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(n * d * 4),
-                "d2h_bytes_per_step": int(n * K * 8)},
+                "d2h_bytes_per_step": int(n * K * 8), "ms_per_step": e2e_ms_steps,
+                "rows_streamed_during_join": e2e_streamed},
         "gpu_launches": launches,
         "roofline": roofline,
         "clocks": clk,
