@@ -130,7 +130,7 @@ def main(argv=None) -> int:
     ap.add_argument("--quantile", type=float, default=0.9)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--holdout", type=int, default=4)
-    ap.add_argument("--out", default="gpurun_out")
+    ap.add_argument("--out", default="radius_model_out")
     a = ap.parse_args(argv)
     os.makedirs(a.out, exist_ok=True)
     rng = np.random.default_rng(a.seed)
