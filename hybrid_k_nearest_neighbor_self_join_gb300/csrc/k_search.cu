@@ -45,6 +45,11 @@ namespace {
 
 constexpr int SEARCH_THREADS = 256;  // largest block; the launch may use fewer warps
 constexpr int QCHUNK = 4;            // default queries per work fetch
+// per-query radii: queries per work fetch up to three indexed dimensions
+// (2 measured best on 2-D and 3-D joins) and beyond (1: uneven work per query)
+#ifndef KNNSJ_QCHUNK_PER_QUERY_RADIUS_LO
+#define KNNSJ_QCHUNK_PER_QUERY_RADIUS_LO 2
+#endif
 #ifndef KNNSJ_QCHUNK_PER_QUERY_RADIUS
 #define KNNSJ_QCHUNK_PER_QUERY_RADIUS 1
 #endif
@@ -1096,7 +1101,9 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s) {
     p.B = (uint32_t)a.shape.buffer;
   // per-query radii make the work per query uneven: finer work fetching
   p.qchunk = a.shape.qchunk > 0 ? (uint32_t)a.shape.qchunk
-                                : (uint32_t)(a.qradius ? KNNSJ_QCHUNK_PER_QUERY_RADIUS : QCHUNK);
+                                : (uint32_t)(!a.qradius               ? QCHUNK
+                                             : a.grid.geom.di <= 3 ? KNNSJ_QCHUNK_PER_QUERY_RADIUS_LO
+                                                                   : KNNSJ_QCHUNK_PER_QUERY_RADIUS);
   const int wpb = a.shape.warps_per_block;
   p.qlist = a.qlist;
   p.nq = a.nq;
