@@ -144,9 +144,13 @@ void KNNJoinPy(float* dataset, unsigned int NUMPOINTS, unsigned int kNN, unsigne
 #endif
 
 /* Status-returning self-join on HOST buffers (same pipeline as KNNJoinPy,
- * dtype chosen per call).  data: row-major n x d; outputs as above.  Pinned
- * (cudaHostAlloc / cudaHostRegister) buffers are copied asynchronously;
- * pageable ones through staging.  stats may be NULL. */
+ * dtype chosen per call).  data: row-major n x d; outputs as above.  When
+ * both outputs are pinned (cudaHostAlloc / cudaHostRegister) and n >= 2^18,
+ * rows are copied into them while the join runs (KNNSJ_ROW_CHUNKS blocks of
+ * query ids, default 32; rows finished by later passes are written at the
+ * end); pageable outputs get one copy through staging after the join.  The
+ * call returns when every row is in place, also on error (no copy is left
+ * in flight).  stats may be NULL. */
 knnsj_status knnsj_selfjoin(const void* data, knnsj_dtype dtype, uint64_t n, uint32_t d,
                             uint32_t k, const knnsj_options* opts, int32_t* out_ids,
                             void* out_dists, knnsj_stats* stats);
