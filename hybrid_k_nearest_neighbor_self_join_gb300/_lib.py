@@ -100,7 +100,8 @@ class Stats(ctypes.Structure):
         ("ms_search_kernels", ctypes.c_double),
         ("search_alg_bytes", ctypes.c_double),
         ("search_alg_flops", ctypes.c_double),
-        ("reserved", ctypes.c_double * 8),
+        ("radius_model_error", ctypes.c_double),
+        ("reserved", ctypes.c_double * 7),
     ]
 
     @classmethod

@@ -436,6 +436,10 @@ void fixed_scratch_join(const T* data, uint64_t n, uint32_t d, uint32_t k, JoinC
   f.w.attach_arena(&f.arena);
   cfg.dense_cells_cap = 4ull * n;  // keeps the dense cell table within the array
   const cudaStream_t s = 0;
+  struct Forbid {  // a buffer the array does not cover fails instead of allocating
+    Forbid() { g_forbid_alloc = true; }
+    ~Forbid() { g_forbid_alloc = false; }
+  } forbid;
   run_join<T>(f.w, cfg, data, nullptr, n, d, k, out_ids, out_d, nullptr, s);
   KNNSJ_CUDA(cudaStreamSynchronize(s));
 }

@@ -35,6 +35,7 @@
 namespace knnsj {
 
 thread_local unsigned long long g_launches = 0;
+thread_local bool g_forbid_alloc = false;
 
 void* Arena::take(size_t bytes) {
   const size_t at = (used + 255) & ~(size_t)255;
@@ -60,12 +61,18 @@ void* DevBuf::get(size_t need) {
   if (need == 0) need = 16;
   if (arena) {
     if (need > bytes) {
-      p = arena->take(need);
+      unsigned char* b = (unsigned char*)p;
+      if (b && b + bytes == arena->base + arena->used && (size_t)(b - arena->base) + need <= arena->cap) {
+        arena->used = (size_t)(b - arena->base) + need;  // the last block carved grows in place
+      } else {
+        p = arena->take(need);
+      }
       bytes = need;
     }
     return p;
   }
   if (need > bytes) {
+    if (g_forbid_alloc) throw StatusError{KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH, "buffer outside the fixed scratch array"};
     if (p) cudaFree(p);
     p = nullptr;
     bytes = 0;
@@ -127,6 +134,7 @@ void Workspace::pinned_release() {
 
 void* Workspace::pinned(size_t need) {
   if (need > h_pinned_bytes) {
+    if (g_forbid_alloc) throw StatusError{KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH, "pinned buffer in a fixed-scratch join"};
     pinned_release();
     KNNSJ_CUDA(cudaMallocHost(&h_pinned, need));
     h_pinned_bytes = need;
@@ -135,12 +143,14 @@ void* Workspace::pinned(size_t need) {
 }
 
 void Workspace::ensure_stream() {
+  if (g_forbid_alloc && !stream) throw StatusError{KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH, "stream in a fixed-scratch join"};
   if (!stream) KNNSJ_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   for (auto& e : ev)
     if (!e) KNNSJ_CUDA(cudaEventCreate(&e));
 }
 
 void Workspace::ensure_copy_stream() {
+  if (g_forbid_alloc) throw StatusError{KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH, "copy stream in a fixed-scratch join"};
   if (!copy_stream) KNNSJ_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
   for (auto& e : chunk_ev)
     if (!e) KNNSJ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -311,7 +321,8 @@ static void build_grid(Workspace& w, const JoinConfig& cfg, uint64_t n, uint32_t
   const unsigned long long dense_limit =
       cfg.dense_cells_cap ? cfg.dense_cells_cap : std::max<unsigned long long>(4ull * n, 1ull << 24);
   out->dense = (cfg.dense_mode != 0) && (g.total_cells <= dense_limit) && g.total_cells < (1ull << 31);
-  if (cfg.dense_mode == 2) out->dense = g.total_cells < (1ull << 31);
+  // (forced dense tables still respect an explicit cap: a fixed scratch array sets one)
+  if (cfg.dense_mode == 2) out->dense = g.total_cells < (1ull << 31) && (!cfg.dense_cells_cap || g.total_cells <= dense_limit);
   out->dstart = nullptr;
   if (out->dense) {
     uint32_t* dstart = (uint32_t*)w.dstart.get((g.total_cells + 1) * 4);
@@ -983,8 +994,8 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   uint32_t mlp_err = 0;
   read_small(w, &cand, &sm->cand, 8, s);
   if (qrad) read_small(w, &mlp_err, &sm->mlp_err, 4, s);
-  if (mlp_err)  // rows are still exact: the affected queries started at eps0
-    fprintf(stderr, "knnsj: the tensor-core radius model timed out; those queries started at eps0\n");
+  if (mlp_err && cfg.verbose)  // rows are still exact: the affected queries started at eps0
+    fprintf(stderr, "knnsj: the tensor-core radius model timed out (%u); those queries started at eps0\n", mlp_err);
   if (st) {
     st->iterations = iter;
     st->regrids = regrids;
@@ -995,6 +1006,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     st->ms_search_kernels = kernel_ms;
     st->search_alg_bytes = alg_bytes;
     st->search_alg_flops = 3.0 * d * (double)cand;
+    st->radius_model_error = (double)mlp_err;
     const float a01 = elapsed(0, 1), a12 = elapsed(1, 2);
     st->ms_prep = a01;
     st->ms_search = a12;

@@ -146,8 +146,21 @@ struct PredictSrc {
 
 template <typename Src>
 __global__ void __launch_bounds__(TC_ROWS) mlp_tc_kernel(Src src, const float* __restrict__ model, uint64_t n,
-                                                          uint32_t* err) {
-  mlp_tc_tiles(src, model, n, err);
+                                                          uint32_t* err, TcCtl ctl) {
+  mlp_tc_tiles(src, model, n, err, ctl);
+}
+
+// KNNSJ_TEST_MLP_TIMEOUT=1 (tests only): the tensor-core MLP issues no MMA and
+// waits at most 1024 polls, so every tile takes the timeout path (eps0
+// radii for a join, NaN predictions, the error flag set).
+static TcCtl tc_ctl() {
+  TcCtl c;
+  const char* e = std::getenv("KNNSJ_TEST_MLP_TIMEOUT");
+  if (e && std::atoi(e) == 1) {
+    c.no_issue = 1;
+    c.wait_limit = 1024;
+  }
+  return c;
 }
 
 template <typename Src>
@@ -168,7 +181,7 @@ void launch_mlp_tc(const Src& src, const float* model, uint64_t n, uint32_t* err
   const uint64_t tiles = (n + TC_ROWS - 1) / TC_ROWS;
   uint64_t blocks = (uint64_t)std::max(per_sm, 1) * (uint64_t)std::max(sm_count, 1);
   if (blocks > tiles) blocks = tiles;
-  mlp_tc_kernel<Src><<<(unsigned)blocks, TC_ROWS, 0, s>>>(src, model, n, err);
+  mlp_tc_kernel<Src><<<(unsigned)blocks, TC_ROWS, 0, s>>>(src, model, n, err, tc_ctl());
   KNNSJ_CHECK_LAUNCH();
 }
 

@@ -33,6 +33,10 @@ struct StatusError {
 // Kernel launches of this host thread since the last reset (reported in
 // knnsj_stats; batched joins run sets on several host threads).
 extern thread_local unsigned long long g_launches;
+// Set while a fixed-scratch join runs on this thread: any cudaMalloc-backed
+// buffer, pinned host buffer or stream creation then fails with
+// KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH instead of allocating.
+extern thread_local bool g_forbid_alloc;
 #define KNNSJ_CHECK_LAUNCH()                 \
   do {                                       \
     KNNSJ_CUDA(cudaGetLastError());          \

@@ -20,9 +20,15 @@
 // byte offset) and consecutive 8-row groups K/8 * 128 bytes apart (stride
 // byte offset).
 //
-// Every wait on the mbarrier is bounded.  On a timeout the CTA records an
-// error, falls back to the plain eps0 radius for its queries (any radius
-// gives exact results), waits once more, frees its TMEM and stops.
+// Every wait on the mbarrier is bounded.  The parity a wait uses flips only
+// after every thread of the CTA saw that phase complete, so after a timeout
+// `phase` still names the commit that has not been seen to complete.  On a
+// timeout the CTA records an error (1), falls back to the plain eps0 radius
+// for its queries (any radius gives exact results), waits once more, bounded,
+// on that same phase when a commit is in flight -- recording error 2 if the
+// tensor core still has not finished -- then frees its TMEM and stops.
+// TcCtl::no_issue (a test switch) makes thread 0 skip the MMAs and their
+// commit: nothing is then in flight, and the first bounded wait runs out.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -35,6 +41,12 @@ constexpr int TC_ROWS = 128;   // queries per tile = MMA M
 constexpr int TC_K1 = 32;      // features padded to two K = 16 steps
 constexpr int TC_TMEM_COLS = 64;
 constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;  // mbarrier polls before giving up
+
+// Wait bound and the test switch of one launch.
+struct TcCtl {
+  uint32_t wait_limit = TC_WAIT_LIMIT;  // mbarrier polls before a wait gives up
+  uint32_t no_issue = 0;                // 1: issue no MMA and no commit (tests the timeout path)
+};
 
 // shared memory of one CTA (bytes)
 constexpr int TC_OFF_A1 = 0;                          // 128 x 32 bf16
@@ -74,9 +86,9 @@ __device__ __forceinline__ void tc_commit(uint32_t bar) {
                : "memory");
 }
 
-// Polls the mbarrier for the given phase; false after TC_WAIT_LIMIT polls.
-__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t phase) {
-  for (uint32_t it = 0; it < TC_WAIT_LIMIT; it++) {
+// Polls the mbarrier for the given phase parity; false after `limit` polls.
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t phase, uint32_t limit) {
+  for (uint32_t it = 0; it < limit; it++) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -122,7 +134,7 @@ __device__ __forceinline__ void tc_put8(unsigned char* base, uint32_t row, uint3
 // features (features(i, f)) and receives its log-radius (store(i, y)) or,
 // after a timeout, the fallback (fallback(i)).
 template <typename Src>
-__device__ void mlp_tc_tiles(Src& src, const float* __restrict__ model, uint64_t n, uint32_t* err) {
+__device__ void mlp_tc_tiles(Src& src, const float* __restrict__ model, uint64_t n, uint32_t* err, TcCtl ctl) {
   __shared__ __align__(128) unsigned char sm[TC_SMEM];
   const uint32_t tid = threadIdx.x, warp = tid >> 5;
   float* prm = reinterpret_cast<float*>(sm + TC_OFF_P);
@@ -175,7 +187,8 @@ __device__ void mlp_tc_tiles(Src& src, const float* __restrict__ model, uint64_t
   const float b3 = w3[NHID];
   const uint32_t a1 = tc_saddr(sm + TC_OFF_A1), a2 = tc_saddr(sm + TC_OFF_A2);
   const uint32_t bb1 = tc_saddr(sm + TC_OFF_B1), bb2 = tc_saddr(sm + TC_OFF_B2);
-  uint32_t phase = 0;
+  uint32_t phase = 0;       // parity of the next completion to wait for
+  bool inflight = false;    // a commit has been issued whose completion was not yet seen by all
   bool failed = false;
   const uint64_t ntiles = (n + TC_ROWS - 1) / TC_ROWS;
   uint64_t tile = blockIdx.x;
@@ -200,7 +213,7 @@ __device__ void mlp_tc_tiles(Src& src, const float* __restrict__ model, uint64_t
     tc_fence_before();
     __syncthreads();
     // 2. first layer
-    if (tid == 0) {
+    if (tid == 0 && !ctl.no_issue) {
       tc_fence_after();
 #pragma unroll
       for (int s = 0; s < TC_K1 / 16; s++)
@@ -208,9 +221,13 @@ __device__ void mlp_tc_tiles(Src& src, const float* __restrict__ model, uint64_t
                s > 0);
       tc_commit(bar);
     }
-    bool ok = tc_wait(bar, phase);
-    phase ^= 1u;
+    inflight = !ctl.no_issue;
+    bool ok = tc_wait(bar, phase, ctl.wait_limit);
     ok = __syncthreads_and(ok);  // uniform: tcgen05.ld is warp-collective
+    if (ok) {                    // every thread saw this phase complete
+      phase ^= 1u;
+      inflight = false;
+    }
     tc_fence_after();
     // 3. ReLU(h + b1) into A2
     if (ok) {
@@ -229,7 +246,7 @@ __device__ void mlp_tc_tiles(Src& src, const float* __restrict__ model, uint64_t
     tc_fence_before();
     ok = __syncthreads_and(ok);
     // 4. second layer, into the same TMEM columns
-    if (ok && tid == 0) {
+    if (ok && tid == 0 && !ctl.no_issue) {
       tc_fence_after();
 #pragma unroll
       for (int s = 0; s < NHID / 16; s++)
@@ -237,9 +254,14 @@ __device__ void mlp_tc_tiles(Src& src, const float* __restrict__ model, uint64_t
                s > 0);
       tc_commit(bar);
     }
-    if (ok) {
-      ok = tc_wait(bar, phase);
-      phase ^= 1u;
+    if (ok) {  // (ok is uniform here: every thread takes this branch or none)
+      inflight = !ctl.no_issue;
+      const bool seen = __syncthreads_and(tc_wait(bar, phase, ctl.wait_limit));
+      if (seen) {
+        phase ^= 1u;
+        inflight = false;
+      }
+      ok = seen;
     }
     ok = __syncthreads_and(ok);
     tc_fence_after();
@@ -260,10 +282,16 @@ __device__ void mlp_tc_tiles(Src& src, const float* __restrict__ model, uint64_t
     ok = __syncthreads_and(ok);
     if (!ok) {
       // an MMA did not complete in time: plain radius for this tile, error
-      // recorded, one more bounded wait for the tensor core, then stop
+      // recorded; if a commit is in flight, one more bounded wait on the
+      // phase that timed out (so that TMEM is freed only once the tensor core
+      // is done with it), then stop
       if (valid) src.fallback(i);
-      if (tid == 0) atomicExch(err, 1u);
-      tc_wait(bar, phase);
+      if (tid == 0) atomicMax(err, 1u);
+      if (inflight) {
+        const bool drained = __syncthreads_and(tc_wait(bar, phase, ctl.wait_limit));
+        if (!drained && tid == 0) atomicMax(err, 2u);  // TMEM released with the MMA unconfirmed
+        inflight = false;
+      }
       failed = true;
     }
   }

@@ -102,7 +102,11 @@ typedef struct {
   double search_alg_bytes;   /* algorithmic bytes of all search passes:
                                 sum over passes of N*d*s + Q*d*s + accepted*(k+1)*(4+s) */
   double search_alg_flops;   /* 3*d per scanned candidate */
-  double reserved[8];
+  double radius_model_error; /* KNNSJ_RADIUS_LEARNED: 0 ok; 1 the tensor-core radius model
+                                timed out and the affected queries started at eps0 (rows stay
+                                exact); 2 as 1, and a timed-out MMA was still unconfirmed when
+                                its tensor memory was released */
+  double reserved[7];
 } knnsj_stats;
 
 /* One independent dataset of a batched call. */
@@ -162,23 +166,25 @@ knnsj_status knnsj_selfjoin_device(const void* d_data, knnsj_dtype dtype, uint64
                                    int32_t* d_out_ids, void* d_out_dists, knnsj_stats* stats);
 
 /* No counterpart in the reference.  The device-buffer self-join for callers
- * that must not allocate GPU memory: code running inside CUDA stream capture
- * (where cudaMalloc is not allowed), allocator-managed runtimes that forbid
- * raw cudaMalloc/cudaFree, and hosts that fix every device allocation up
- * front.  It calls no cudaMalloc, cudaFree, stream or event creation and no
- * allocating library routine; all scratch comes from one static device array
- * of KNNSJ_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds
- * until the process exits.  Limits: n <= KNNSJ_NOALLOC_MAX_POINTS, d <= 8,
- * k+1 <= 128; larger problems return KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH.
- * The caller passes the input and output device buffers, as for
- * knnsj_selfjoin_device, and gets the same results.  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress); make
- * that first call before any stream capture.  The call runs on the legacy
- * default stream and returns when the join is done.  Every call reuses the
- * same array, which keeps the previous call's contents (the join clears what
- * must start at zero); calls whose GPU work overlapped would race on it, so
- * the library takes its call lock and finishes each call's GPU work before
- * returning. */
+ * that must not allocate GPU memory: runtimes whose own allocator owns the
+ * device memory and forbids raw cudaMalloc/cudaFree, and hosts that fix every
+ * device allocation up front (an allocation in the middle of their work could
+ * fail or fragment their pool).  It calls no cudaMalloc, cudaFree, stream or
+ * event creation and no allocating library routine; all scratch comes from
+ * one static device array of KNNSJ_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading this library holds until the process exits.  Limits:
+ * n <= KNNSJ_NOALLOC_MAX_POINTS, d <= 8, k+1 <= 128; larger problems return
+ * KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH, and so does any step of the join that
+ * would need memory beyond the array.  The caller passes the input and output
+ * device buffers, as for knnsj_selfjoin_device, and gets the same results.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The call runs on the legacy default stream, reads a few small values back
+ * to the host while it runs (stream synchronisations), and returns when the
+ * join is done.  Every call reuses the same array, which keeps the previous
+ * call's contents (the join clears what must start at zero); calls whose GPU
+ * work overlapped would race on it, so the library takes its call lock and
+ * finishes each call's GPU work before returning. */
 #define KNNSJ_NOALLOC_SCRATCH_BYTES (24u << 20)
 #define KNNSJ_NOALLOC_MAX_POINTS 65536u
 knnsj_status knnsj_selfjoin_device_noalloc(const void* d_data, knnsj_dtype dtype, uint64_t n, uint32_t d,
