@@ -15,7 +15,7 @@ import numpy as np
 from . import _lib
 from ._lib import KnnsjError, Options, Stats
 
-__all__ = ["selfjoin", "selfjoin_device", "selfjoin_batched", "reorder_dims", "grid_dims", "read_csv",
+__all__ = ["selfjoin", "selfjoin_device", "selfjoin_batched", "reorder_dims", "grid_dims", "read_csv", "read_binary",
            "write_knn_out", "write_outlier_scores", "version", "KnnsjError", "Options", "Stats"]
 
 
@@ -39,7 +39,7 @@ RADIUS_LEARNED = _lib.KNNSJ_RADIUS_LEARNED
 def selfjoin(data: np.ndarray, k: int, *, num_indexed_dims: int = 0, beta: float | None = None,
              reorder: bool = True, radius_mode: int = 0, max_iterations: int = 0, device: int = -1,
              radius_offset: float = 0.0, out_ids: np.ndarray | None = None,
-             out_dists: np.ndarray | None = None, return_stats: bool = False):
+             out_dists: np.ndarray | None = None, return_stats: bool = False, device_table_mb: int = 0):
     """Exact kNN self-join of row-major host data (N x d, float32/float64).
 
     Returns (ids, dists), each (N, k+1): row q holds the k+1 nearest points of
@@ -54,7 +54,7 @@ def selfjoin(data: np.ndarray, k: int, *, num_indexed_dims: int = 0, beta: float
     ids = out_ids if out_ids is not None else np.empty((n, K), np.int32)
     dists = out_dists if out_dists is not None else np.empty((n, K), x.dtype)
     opts = Options.make(num_indexed_dims, beta, reorder, radius_mode, max_iterations, device,
-                        radius_offset=radius_offset)
+                        radius_offset=radius_offset, device_table_mb=device_table_mb)
     st = Stats.make()
     lib = _lib.load()
     rc = lib.knnsj_selfjoin(x.ctypes.data, _dtype_code(x.dtype), n, d, k, ctypes.byref(opts),
@@ -155,6 +155,17 @@ def read_csv(path: str, d: int, dtype=np.float32) -> np.ndarray:
     _lib.check(lib.knnsj_read_csv(path.encode(), code, d, None, ctypes.byref(n)), path)
     out = np.empty((n.value, d), dtype)
     _lib.check(lib.knnsj_read_csv(path.encode(), code, d, out.ctypes.data, ctypes.byref(n)), path)
+    return out
+
+
+def read_binary(path: str, d: int, dtype=np.float32) -> np.ndarray:
+    """Points from a .npy file or raw little-endian values (knnsj_read_binary)."""
+    lib = _lib.load()
+    n = ctypes.c_uint64(0)
+    code = _dtype_code(dtype)
+    _lib.check(lib.knnsj_read_binary(path.encode(), code, d, None, ctypes.byref(n)), path)
+    out = np.empty((n.value, d), dtype)
+    _lib.check(lib.knnsj_read_binary(path.encode(), code, d, out.ctypes.data, ctypes.byref(n)), path)
     return out
 
 

@@ -44,12 +44,13 @@ class Options(ctypes.Structure):
         ("device", ctypes.c_int32),
         ("verbose", ctypes.c_int32),
         ("radius_offset", ctypes.c_double),
-        ("reserved", ctypes.c_int32 * 8),
+        ("device_table_mb", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 7),
     ]
 
     @classmethod
     def make(cls, num_indexed_dims=0, beta=None, reorder=True, radius_mode=0, max_iterations=0,
-             device=-1, verbose=0, radius_offset=0.0):
+             device=-1, verbose=0, radius_offset=0.0, device_table_mb=0):
         o = cls()
         o.struct_size = ctypes.sizeof(cls)
         o.num_indexed_dims = int(num_indexed_dims or 0)
@@ -60,6 +61,7 @@ class Options(ctypes.Structure):
         o.device = int(device)
         o.verbose = int(verbose)
         o.radius_offset = float(radius_offset)
+        o.device_table_mb = int(device_table_mb)
         return o
 
 
@@ -101,7 +103,8 @@ class Stats(ctypes.Structure):
         ("search_alg_bytes", ctypes.c_double),
         ("search_alg_flops", ctypes.c_double),
         ("radius_model_error", ctypes.c_double),
-        ("reserved", ctypes.c_double * 7),
+        ("tile_handovers", ctypes.c_double),
+        ("reserved", ctypes.c_double * 6),
     ]
 
     @classmethod
@@ -160,6 +163,8 @@ _SIGNATURES = [
                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
     ("knnsj_read_csv", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_void_p,
                                       ctypes.POINTER(ctypes.c_uint64)]),
+    ("knnsj_read_binary", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_void_p,
+                                         ctypes.POINTER(ctypes.c_uint64)]),
     ("knnsj_write_knn_out", ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint64, ctypes.c_uint32,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ("knnsj_write_outlier_scores", ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint64, ctypes.c_uint32,

@@ -53,6 +53,10 @@ knnsj_status make_config(const knnsj_options* o, uint32_t d, JoinConfig* c) {
   if (const char* e = env("KNNSJ_FLOAT_PREFILTER")) c->float_prefilter = std::atoi(e);
   if (const char* e = env("KNNSJ_ROW_CHUNKS")) c->row_chunks = std::atoi(e);
   if (const char* e = env("KNNSJ_TAIL_BRUTE")) c->tail_brute = std::atoi(e);
+  if (const char* e = env("KNNSJ_TILE")) c->tile_search = std::atoi(e);
+  if (const char* e = env("KNNSJ_TILE_FINE")) c->tile_fine = std::max(1, std::atoi(e));
+  if (const char* e = env("KNNSJ_DIRECT_ROWS")) c->direct_rows = std::atoi(e);
+  if (const char* e = env("KNNSJ_DEVICE_TABLE_MB")) c->device_table_cap = (unsigned long long)std::atoll(e) << 20;
   if (const char* e = env("KNNSJ_SEARCH_SHAPE")) {  // "warps,qchunk,buffer" (0 = default)
     int a = 0, b = 0, bb = 0;
     if (std::sscanf(e, "%d,%d,%d", &a, &b, &bb) >= 1) {
@@ -71,6 +75,8 @@ knnsj_status make_config(const knnsj_options* o, uint32_t d, JoinConfig* c) {
     if (o->verbose) c->verbose = o->verbose;
     if (o->struct_size >= offsetof(knnsj_options, radius_offset) + sizeof(double))
       c->radius_offset = o->radius_offset;
+    if (o->struct_size >= offsetof(knnsj_options, device_table_mb) + sizeof(int32_t) && o->device_table_mb > 0)
+      c->device_table_cap = (unsigned long long)o->device_table_mb << 20;
   }
   if (const char* e = env("KNNSJ_RADIUS_MODE")) c->radius_mode = std::atoi(e);
   if (c->num_indexed_dims == 0 || c->num_indexed_dims > d) c->num_indexed_dims = d < 6 ? d : 6;
@@ -150,24 +156,112 @@ void init_stats(knnsj_stats* st) {
   st->struct_size = sz ? sz : (uint32_t)sizeof(*st);
 }
 
-// Outputs of fewer rows go back in one copy after the join.
+// Where the rows of a host-pointer call go:
+//  * direct rows (default): when both output buffers are pinned and mapped
+//    into the device's address space, the search kernels write every row
+//    straight into them (no device result table, no copy after the join);
+//  * when the device result table would not fit (more than the free device
+//    memory less a margin, or cfg.device_table_cap), pageable output buffers
+//    are registered with the device for the duration of the call and take
+//    their rows the same way -- the device then holds no result table at
+//    all, which bounds device memory by the input and the index;
+//  * otherwise a device result table, copied out after the join (or streamed
+//    out in blocks of query ids while the join runs, cfg.row_chunks >= 2 with
+//    direct rows off).
 constexpr uint64_t ROW_STREAM_MIN_ROWS = 1u << 18;
+
+// Device-visible address of a host buffer, when it is pinned and mapped.
+void* mapped_host_pointer(void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // an unregistered pointer is not an error here
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Registers pageable host buffers with the device for one call (mapped);
+// unregisters on destruction.
+struct HostRegistration {
+  cudaStream_t stream = nullptr;  // finished before the buffers are unregistered
+  std::vector<void*> regs;
+  bool add(void* p, size_t bytes) {
+    if (cudaHostRegister(p, bytes, cudaHostRegisterMapped) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    regs.push_back(p);
+    return true;
+  }
+  ~HostRegistration() {
+    if (!regs.empty() && stream) cudaStreamSynchronize(stream);
+    for (void* p : regs) cudaHostUnregister(p);
+  }
+};
+
+// Waits for a stream when leaving a scope, also on an error: no kernel is
+// left writing into the caller's buffers after the call returns.
+struct SyncOnExit {
+  cudaStream_t s;
+  ~SyncOnExit() { cudaStreamSynchronize(s); }
+};
 
 template <typename T>
 void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t k, const JoinConfig& cfg,
                   int32_t* out_ids, T* out_d, knnsj_stats* st, bool checksum) {
   cudaStream_t s = w.stream;
   const uint64_t K = (uint64_t)k + 1;
+  const uint64_t table_bytes = n * K * (4 + sizeof(T));
   T* din = (T*)w.in.get(n * d * sizeof(T));
-  int32_t* dids = (int32_t*)w.ids.get(n * K * 4);
-  T* ddist = (T*)w.dists.get(n * K * sizeof(T));
   cudaEvent_t t0, t1;
   KNNSJ_CUDA(cudaEventCreate(&t0));
   KNNSJ_CUDA(cudaEventCreate(&t1));
   KNNSJ_CUDA(cudaEventRecord(t0, s));
   KNNSJ_CUDA(cudaMemcpyAsync(din, data, n * d * sizeof(T), cudaMemcpyHostToDevice, s));
   KNNSJ_CUDA(cudaEventRecord(t1, s));
-  // pinned output buffers take their rows while the join runs
+  double* rowsum = (st && checksum) ? (double*)w.rowsum.get(n * 8) : nullptr;
+  // 1. direct rows into pinned buffers, or into pageable buffers registered
+  // for this call when the result table does not fit on the device
+  int32_t* ids_dev = nullptr;
+  T* d_dev = nullptr;
+  HostRegistration reg;
+  reg.stream = s;
+  if (cfg.direct_rows) {
+    ids_dev = (int32_t*)mapped_host_pointer(out_ids);
+    d_dev = (T*)mapped_host_pointer(out_d);
+    if (!ids_dev || !d_dev) {
+      ids_dev = nullptr;
+      d_dev = nullptr;
+      size_t free_b = 0, total_b = 0;
+      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) cudaGetLastError();
+      const uint64_t cap = cfg.device_table_cap ? cfg.device_table_cap
+                                                : (free_b > (2ull << 30) ? (uint64_t)free_b - (2ull << 30) : 0ull);
+      if (table_bytes > cap && reg.add(out_ids, n * K * 4) && reg.add(out_d, n * K * sizeof(T))) {
+        ids_dev = (int32_t*)mapped_host_pointer(out_ids);
+        d_dev = (T*)mapped_host_pointer(out_d);
+        if (!ids_dev || !d_dev) ids_dev = nullptr, d_dev = nullptr;
+      }
+    }
+  }
+  if (ids_dev && d_dev) {
+    SyncOnExit guard{s};
+    run_join<T>(w, cfg, din, data, n, d, k, ids_dev, d_dev, st, s, nullptr, rowsum);
+    KNNSJ_CUDA(cudaStreamSynchronize(s));
+    if (st) {
+      float a = 0;
+      cudaEventElapsedTime(&a, t0, t1);
+      st->ms_transfer = a;  // the rows needed no copy
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (cfg.verbose && st)
+      fprintf(stderr, "knnsj: n=%llu d=%u k=%u rows written to host memory; prep=%.3f ms search=%.3f ms\n",
+              (unsigned long long)n, d, k, st->ms_prep, st->ms_search);
+    return;
+  }
+  // 2. a device result table, streamed or copied after the join
+  int32_t* dids = (int32_t*)w.ids.get(n * K * 4);
+  T* ddist = (T*)w.dists.get(n * K * sizeof(T));
   RowStream rs;
   RowStream* rsp = nullptr;
   if (cfg.row_chunks >= 2 && n >= ROW_STREAM_MIN_ROWS) {
@@ -179,7 +273,6 @@ void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t 
       rs.ids_dev = ai.devicePointer;
       rs.d_dev = ad.devicePointer;
       rs.chunks = cfg.row_chunks;
-      rs.checksum = st && checksum;
       rsp = &rs;
     }
     cudaGetLastError();  // an unregistered pointer is not an error here
@@ -193,9 +286,8 @@ void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t 
     }
   } copy_wait;
   if (rsp) copy_wait.w = &w;
-  run_join<T>(w, cfg, din, data, n, d, k, dids, ddist, st, s, rsp);
-  const bool streamed = rsp && rsp->active;  // rows already in place, checksum taken
-  if (st && checksum) st->total_distance = streamed ? rsp->total_distance : device_checksum<T>(w, ddist, n * K, s);
+  run_join<T>(w, cfg, din, data, n, d, k, dids, ddist, st, s, rsp, rowsum);
+  const bool streamed = rsp && rsp->active;  // rows already in place
   cudaEvent_t t2, t3;
   KNNSJ_CUDA(cudaEventCreate(&t2));
   KNNSJ_CUDA(cudaEventCreate(&t3));

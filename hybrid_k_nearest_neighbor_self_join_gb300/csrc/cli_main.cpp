@@ -10,7 +10,9 @@
 // (KNNSJ_PRINTNEIGHBORTABLE, KNNSJ_PRINTOUTLIERSCORES; default 0) or fixed
 // with -D at build time; when set, KNN_out.txt / KNN_out_distances.txt /
 // KNN_outlier_scores.txt are written to the working directory.  One line per
-// run is appended to gpu_stats.txt, as main.cu:472-489 does.
+// run is appended to gpu_stats.txt, as main.cu:472-489 does.  A FNAME ending
+// in .npy, .bin or .raw is read as binary (NumPy array or raw values of the
+// build's DTYPE) instead of CSV.
 
 #include <chrono>
 #include <cstdio>
@@ -56,14 +58,24 @@ int main(int argc, char* argv[]) {
     std::fprintf(stderr, "knnsj: DIM must be positive\n");
     return 1;
   }
+  // FNAME ending in .npy, .bin or .raw is read as binary (knnsj_read_binary),
+  // anything else as the reference's CSV
+  auto ends_with = [&](const char* suf) {
+    const size_t a = std::strlen(fname), b = std::strlen(suf);
+    return a >= b && std::strcmp(fname + a - b, suf) == 0;
+  };
+  const bool binary = ends_with(".npy") || ends_with(".bin") || ends_with(".raw");
+  auto read = [&](void* out, uint64_t* cnt) {
+    return binary ? knnsj_read_binary(fname, kDtype, NDIM, out, cnt) : knnsj_read_csv(fname, kDtype, NDIM, out, cnt);
+  };
   uint64_t n = 0;
-  knnsj_status s = knnsj_read_csv(fname, kDtype, NDIM, nullptr, &n);
+  knnsj_status s = read(nullptr, &n);
   if (s != KNNSJ_OK) {
     std::fprintf(stderr, "knnsj: cannot read %s: %s\n", fname, knnsj_status_string(s));
     return 1;
   }
   std::vector<dtype_t> data((size_t)n * NDIM);
-  s = knnsj_read_csv(fname, kDtype, NDIM, data.data(), &n);
+  s = read(data.data(), &n);
   if (s != KNNSJ_OK) {
     std::fprintf(stderr, "knnsj: cannot read %s: %s\n", fname, knnsj_status_string(s));
     return 1;

@@ -245,9 +245,159 @@ knnsj_status write_outlier_impl(const char* dir, uint64_t n, uint32_t K, const i
   return KNNSJ_OK;
 }
 
+// ---- binary input: NumPy .npy (format 1.0-3.0) or raw little-endian values ---
+// Neither exists in the reference, which reads CSV only
+// (import_dataset.cpp:50-106); at tens of millions of points a binary file
+// is read in a fraction of the time the text parse takes.
+struct BinLayout {
+  uint64_t offset = 0;   // first data byte
+  uint64_t values = 0;   // values in the file
+  int elem = 0;          // 4 (float32) or 8 (float64)
+  bool ok = false;
+};
+
+// Parses the .npy header (magic, version, header length, the dict with
+// 'descr', 'fortran_order' and 'shape'); raw files are taken as values of
+// the requested type.  Big-endian and Fortran-ordered arrays are refused.
+BinLayout bin_layout(FILE* f, uint64_t fsize, int want_elem) {
+  BinLayout L;
+  unsigned char head[10];
+  const size_t got = std::fread(head, 1, sizeof(head), f);
+  if (got >= 10 && head[0] == 0x93 && std::memcmp(head + 1, "NUMPY", 5) == 0) {
+    const int major = head[6];
+    uint64_t hlen = 0, pre = 0;
+    if (major == 1) {
+      hlen = (uint64_t)head[8] | ((uint64_t)head[9] << 8);
+      pre = 10;
+    } else if (major == 2 || major == 3) {
+      unsigned char b[2];
+      if (std::fread(b, 1, 2, f) != 2) return L;
+      hlen = (uint64_t)head[8] | ((uint64_t)head[9] << 8) | ((uint64_t)b[0] << 16) | ((uint64_t)b[1] << 24);
+      pre = 12;
+    } else {
+      return L;
+    }
+    if (hlen > (1u << 20) || pre + hlen > fsize) return L;
+    std::string h(hlen, '\0');
+    if (std::fseek(f, (long)pre, SEEK_SET) != 0 || std::fread(&h[0], 1, hlen, f) != hlen) return L;
+    const size_t dp = h.find("'descr'");
+    if (dp == std::string::npos) return L;
+    const size_t q1 = h.find('\'', h.find(':', dp) + 1);
+    const size_t q2 = q1 == std::string::npos ? q1 : h.find('\'', q1 + 1);
+    if (q2 == std::string::npos) return L;
+    const std::string descr = h.substr(q1 + 1, q2 - q1 - 1);
+    if (descr == "<f4" || descr == "=f4" || descr == "f4")
+      L.elem = 4;
+    else if (descr == "<f8" || descr == "=f8" || descr == "f8")
+      L.elem = 8;
+    else
+      return L;
+    const size_t fo = h.find("'fortran_order'");
+    if (fo == std::string::npos || h.find("True", fo) < h.find(',', fo)) return L;
+    const size_t sp = h.find("'shape'");
+    if (sp == std::string::npos) return L;
+    const size_t p1 = h.find('(', sp), p2 = h.find(')', sp);
+    if (p1 == std::string::npos || p2 == std::string::npos) return L;
+    uint64_t count = 1;
+    const std::string dims = h.substr(p1 + 1, p2 - p1 - 1);
+    size_t i = 0;
+    bool any = false;
+    while (i < dims.size()) {
+      while (i < dims.size() && (dims[i] == ' ' || dims[i] == ',')) i++;
+      if (i >= dims.size()) break;
+      char* end = nullptr;
+      const unsigned long long v = std::strtoull(dims.c_str() + i, &end, 10);
+      if (end == dims.c_str() + i) return L;
+      count *= v;
+      any = true;
+      i = (size_t)(end - dims.c_str());
+    }
+    if (!any) count = 1;  // a 0-d array holds one value
+    L.offset = pre + hlen;
+    L.values = count;
+    if (L.offset + count * (uint64_t)L.elem > fsize) return L;
+    L.ok = true;
+    return L;
+  }
+  L.offset = 0;
+  L.elem = want_elem;
+  L.values = fsize / (uint64_t)want_elem;
+  L.ok = fsize % (uint64_t)want_elem == 0;
+  return L;
+}
+
+template <typename T>
+knnsj_status read_binary_impl(const char* path, uint32_t d, T* out, uint64_t* n_points) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return KNNSJ_ERR_IO;
+  std::fseek(f, 0, SEEK_END);
+  const long fs = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  if (fs < 0) {
+    std::fclose(f);
+    return KNNSJ_ERR_IO;
+  }
+  const BinLayout L = bin_layout(f, (uint64_t)fs, (int)sizeof(T));
+  std::fclose(f);
+  if (!L.ok) return KNNSJ_ERR_IO;
+  const uint64_t n = L.values / d;  // a trailing partial point is dropped, as the CSV reader does
+  *n_points = n;
+  if (!out) return KNNSJ_OK;
+  const uint64_t total = n * d;
+  // parallel read in 8 MB blocks: each thread opens the file and reads its blocks
+  const uint64_t block = (8u << 20) / (uint64_t)L.elem;
+  const int64_t nblocks = (int64_t)((total + block - 1) / block);
+  int failed = 0;
+#pragma omp parallel reduction(| : failed)
+  {
+    FILE* g = std::fopen(path, "rb");
+    if (!g) failed = 1;
+    std::vector<unsigned char> buf;
+#pragma omp for schedule(dynamic, 4)
+    for (int64_t b = 0; b < nblocks; b++) {
+      if (!g) continue;
+      const uint64_t v0 = (uint64_t)b * block;
+      const uint64_t cnt = std::min<uint64_t>(block, total - v0);
+      if (std::fseek(g, (long)(L.offset + v0 * (uint64_t)L.elem), SEEK_SET) != 0) {
+        failed = 1;
+        continue;
+      }
+      if (L.elem == (int)sizeof(T)) {
+        if (std::fread(out + v0, sizeof(T), cnt, g) != cnt) failed = 1;
+      } else {
+        buf.resize(cnt * (uint64_t)L.elem);
+        if (std::fread(buf.data(), 1, buf.size(), g) != buf.size()) {
+          failed = 1;
+          continue;
+        }
+        for (uint64_t i = 0; i < cnt; i++) {
+          if (L.elem == 4) {
+            float v;
+            std::memcpy(&v, &buf[i * 4], 4);
+            out[v0 + i] = (T)v;
+          } else {
+            double v;
+            std::memcpy(&v, &buf[i * 8], 8);
+            out[v0 + i] = (T)v;  // float64 -> float32: round to nearest
+          }
+        }
+      }
+    }
+    if (g) std::fclose(g);
+  }
+  return failed ? KNNSJ_ERR_IO : KNNSJ_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+knnsj_status knnsj_read_binary(const char* path, knnsj_dtype dtype, uint32_t d, void* out, uint64_t* n_points) {
+  if (!path || !n_points || d == 0) return KNNSJ_ERR_INVALID_ARGUMENT;
+  if (dtype == KNNSJ_F32) return read_binary_impl<float>(path, d, (float*)out, n_points);
+  if (dtype == KNNSJ_F64) return read_binary_impl<double>(path, d, (double*)out, n_points);
+  return KNNSJ_ERR_INVALID_ARGUMENT;
+}
 
 knnsj_status knnsj_reorder_dims(const void* data, knnsj_dtype dtype, uint64_t n, uint32_t d, uint32_t* perm,
                                 void* variances) {

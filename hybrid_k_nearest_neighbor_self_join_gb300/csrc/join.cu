@@ -48,7 +48,8 @@ void* Arena::take(size_t bytes) {
 void Workspace::attach_arena(Arena* a) {
   DevBuf* bufs[] = {&model, &in, &ids, &dists, &xs, &ps, &psf, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
                     &scan_tmp, &flags, &pos, &ckeys, &coff, &dstart, &list0, &list1, &small,
-                    &eps_partial, &eps_sample, &perm, &minmax_part, &qradius, &chunk_list, &patch_rows};
+                    &eps_partial, &eps_sample, &perm, &minmax_part, &qradius, &chunk_list, &patch_rows, &defer_list,
+                    &fps, &fpid, &fdstart, &qorder, &rowsum};
   for (DevBuf* b : bufs) {
     b->arena = a;
     b->p = nullptr;
@@ -106,7 +107,8 @@ void Workspace::release_all() {
   model_version = 0;
   DevBuf* bufs[] = {&model, &in, &ids, &dists, &xs, &ps, &psf, &pid, &keys0, &keys1, &vals0, &vals1, &hist,
                     &scan_tmp, &flags, &pos, &ckeys, &coff, &dstart, &list0, &list1, &small,
-                    &eps_partial, &eps_sample, &perm, &minmax_part, &qradius, &chunk_list, &patch_rows};
+                    &eps_partial, &eps_sample, &perm, &minmax_part, &qradius, &chunk_list, &patch_rows, &defer_list,
+                    &fps, &fpid, &fdstart, &qorder, &rowsum};
   for (DevBuf* b : bufs) b->release();
   if (stream) cudaStreamDestroy(stream);
   stream = nullptr;
@@ -232,7 +234,7 @@ struct SmallDev {  // layout of Workspace::small
   uint32_t nonfinite;
   uint32_t fail_count;
   uint32_t work_counter;
-  uint32_t pad;
+  uint32_t defer_count;  // queries the tile search handed to search_kernel (current launch)
   unsigned long long C;
   unsigned long long cand;
   double avg[2];
@@ -244,6 +246,7 @@ struct SmallDev {  // layout of Workspace::small
   uint32_t mlp_err;  // the tensor-core radius MLP timed out
   uint32_t chunk_fill[MAX_ROW_CHUNKS];  // streamed rows: queries placed per id block
   uint32_t patch_count;                 // streamed rows: first-pass failures
+  unsigned long long defer_total;       // all queries handed over by the tile search in this join
 };
 
 template <typename T>
@@ -386,15 +389,16 @@ __global__ void loop_cond_kernel(const LoopCtl* c, cudaGraphConditionalHandle ha
 }
 
 // Streamed rows: the queries of each block of crow consecutive ids, in the
-// cell order they have in pid (nearby queries stay together), block c at
+// cell order they have in pid, visited in `order` when given (nearby queries
+// stay together), block c at
 // lists[c * crow ...].  Lanes of a warp with the same block take consecutive
 // slots from one atomic.
-__global__ void chunk_lists_kernel(const uint32_t* __restrict__ pid, uint32_t n, uint32_t crow,
-                                   uint32_t* __restrict__ fill, uint32_t* __restrict__ lists) {
+__global__ void chunk_lists_kernel(const uint32_t* __restrict__ pid, const uint32_t* __restrict__ order, uint32_t n,
+                                   uint32_t crow, uint32_t* __restrict__ fill, uint32_t* __restrict__ lists) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool live = i < n;
-  const uint32_t id = live ? pid[i] : 0u;
+  const uint32_t id = live ? pid[order ? order[i] : i] : 0u;
   const uint32_t c = live ? id / crow : 0xffffffffu;
   const unsigned peers = __match_any_sync(0xffffffffu, c);
   const int leader = __ffs(peers) - 1;
@@ -431,7 +435,127 @@ __global__ void patch_rows_kernel(const uint32_t* __restrict__ rows, const uint3
   }
 }
 
+// Adds the tile search's hand-over count to the join's total and clears it
+// for the next launch.
+__global__ void defer_roll_kernel(uint32_t* __restrict__ count, unsigned long long* __restrict__ total) {
+  *total += *count;
+  *count = 0u;
+}
+
 }  // namespace
+
+// Set-up of the tile search for the first pass: the order in which tiles
+// take the queries (Morton order of their eps0 cells, so that 32 consecutive
+// queries are close in every dimension) and the grid the candidates come
+// from (a finer grid of width eps0 / f when its dense table fits).
+template <typename T>
+struct TileSetup {
+  bool on = false;
+  DeviceGrid<T> cand;                 // candidate grid
+  const uint32_t* qorder = nullptr;   // positions of the eps0 grid's cell order, in tile order
+  int fine = 1;                       // eps0 / candidate cell width
+  bool per_query = false;             // search_kernel (one warp per query) on the candidate grid
+};
+
+template <typename T>
+static void prepare_tile(Workspace& w, const JoinConfig& cfg, const DeviceGrid<T>& g, const T* xs, uint64_t n,
+                         uint32_t d, T eps0, const std::vector<T>& mx, TileSetup<T>* t, cudaStream_t s) {
+  const uint32_t di = g.geom.di;
+  // 1. Morton order of the eps0 cells (stable: cell order within a cell)
+  int bits = 1;
+  for (uint32_t j = 0; j < di; j++)
+    while (bits < 21 && (1ull << bits) < (unsigned long long)g.geom.ncell[j]) bits++;
+  GridScratch sc;
+  sc.keys[0] = (unsigned long long*)w.keys0.get(n * 8);
+  sc.keys[1] = (unsigned long long*)w.keys1.get(n * 8);
+  sc.vals[0] = (uint32_t*)w.vals0.get(n * 4);
+  sc.vals[1] = (uint32_t*)w.vals1.get(n * 4);
+  sc.hist_elems = radix_hist_elems(n);
+  sc.hist = (uint32_t*)w.hist.get(sc.hist_elems * 4);
+  sc.scan_tmp_elems = scan_tmp_elems(std::max<size_t>(sc.hist_elems, n + 1));
+  sc.scan_tmp = (uint32_t*)w.scan_tmp.get(sc.scan_tmp_elems * 4);
+  launch_morton_keys<T>(g.ps, n, g.geom, bits, sc.keys[0], sc.vals[0], s);
+  const int cur = radix_sort_pairs(sc, n, bits * (int)di, s);
+  uint32_t* qorder = (uint32_t*)w.qorder.get(n * 4);
+  dev_copy(w, qorder, sc.vals[cur], n * 4, s);
+  t->qorder = qorder;
+  // 2. candidate grid: width eps0 / f, the largest f <= cfg.tile_fine whose
+  // dense table stays within max(8 n, 2^24) cells
+  t->cand = g;
+  t->fine = 1;
+  const unsigned long long limit = std::max<unsigned long long>(8ull * n, 1ull << 24);
+  for (int f = cfg.tile_fine; f >= 2; f--) {
+    GridGeom<T> gf = g.geom;
+    gf.width = (T)((double)eps0 / (double)f);
+    if (!(gf.width > 0)) continue;
+    unsigned long long mult = 1;
+    bool fits = true;
+    for (uint32_t j = 0; j < di && fits; j++) {
+      const T hi = mx[j] + eps0;
+      const T cells = std::ceil((hi - gf.minv[j]) / gf.width);
+      if (!(cells < 4294967295.0)) {
+        fits = false;
+        break;
+      }
+      gf.ncell[j] = std::max<uint32_t>((uint32_t)cells, 1u);
+      gf.mult[j] = mult;
+      if (mult > limit / gf.ncell[j]) fits = false;
+      mult *= gf.ncell[j];
+    }
+    if (!fits || mult > limit) continue;
+    gf.total_cells = mult;
+    uint32_t* tbl = (uint32_t*)w.fdstart.get((mult + 1) * 4);
+    uint32_t* tmp = (uint32_t*)w.scan_tmp.get(std::max(sc.scan_tmp_elems, scan_tmp_elems(mult)) * 4);
+    T* fps = (T*)w.fps.get(n * d * sizeof(T));
+    uint32_t* fpid = (uint32_t*)w.fpid.get(n * 4);
+    launch_counting_grid<T>(xs, n, d, gf, tbl, tmp, fps, fpid, s);
+    t->cand.geom = gf;
+    t->cand.ps = fps;
+    t->cand.psf = nullptr;
+    t->cand.pid = fpid;
+    t->cand.ckeys = nullptr;
+    t->cand.coff = nullptr;
+    t->cand.C = 0;
+    t->cand.dense = 1;
+    t->cand.dstart = tbl;
+    t->fine = f;
+    break;
+  }
+  t->on = true;
+  t->per_query = cfg.tile_search == 2;
+}
+
+// One search pass over the queries of a.qlist (or all points in cell order):
+// the tile search where it is set up, then search_kernel over the queries it
+// handed over, at the same radius on the eps0 grid; otherwise search_kernel
+// alone.
+template <typename T>
+static void first_pass_search(Workspace& w, const SearchLaunch<T>& a, const TileSetup<T>& tile, SmallDev* sm,
+                              cudaStream_t s) {
+  if (tile.on && tile.per_query) {  // search_kernel over the finer candidate grid, queries in its cell order
+    SearchLaunch<T> t = a;
+    t.grid = tile.cand;
+    launch_search<T>(t, w.sm_count, s);
+    return;
+  }
+  if (tile.on) {
+    uint32_t* defer = (uint32_t*)w.defer_list.get(a.n * 4);
+    SearchLaunch<T> t = a;
+    t.grid = tile.cand;
+    t.qps = a.grid.ps;
+    t.qpid = a.grid.pid;
+    t.qorder = tile.qorder;
+    launch_tile_search<T>(t, defer, &sm->defer_count, w.sm_count, s);
+    SearchLaunch<T> b = a;
+    b.qlist = defer;
+    b.nq_dev = &sm->defer_count;
+    launch_search<T>(b, w.sm_count, s);
+    defer_roll_kernel<<<1, 1, 0, s>>>(&sm->defer_count, &sm->defer_total);
+    KNNSJ_CHECK_LAUNCH();
+    return;
+  }
+  launch_search<T>(a, w.sm_count, s);
+}
 
 // Steps 1-4 of the pipeline: dimension order, column transpose, eps0 and
 // the grid index at eps0.
@@ -492,7 +616,7 @@ static void prepare(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T
   launch_eps_avg<T>(xs, n, d, es, s);
   KNNSJ_CUDA(cudaMemsetAsync(sm->hist, 0, sizeof(sm->hist), s));
   struct Head {
-    uint32_t nonfinite, fail_count, work_counter, pad;
+    uint32_t nonfinite, fail_count, work_counter, defer_count;
     unsigned long long C, cand;
     double avg[2];
   } head;
@@ -673,7 +797,8 @@ static bool run_graph_passes(Workspace& w, SearchLaunch<T> a, LoopCtl& c, LoopCt
 
 template <typename T>
 void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
-              uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s, RowStream* rows) {
+              uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s, RowStream* rows,
+              double* rowsum) {
   const uint32_t K = k + 1;
   const uint32_t di = cfg.num_indexed_dims;
   cudaEvent_t* ev = w.ev;
@@ -703,6 +828,11 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
                             (float)cfg.radius_offset, qrad, &sm->mlp_err, w.sm_count, s);
     rmax = (double)P.eps0 * learned_max_cells(di);
   }
+  // 5b. the first pass's tile search (2-D / 3-D float data, all indexed)
+  TileSetup<T> tile;
+  const bool will_stream = rows && rows->chunks >= 2 && n >= (uint64_t)rows->chunks;
+  if (cfg.tile_search && !will_stream && tile_search_applies(d, di, K, P.grid.dense, sizeof(T)))
+    prepare_tile<T>(w, cfg, P.grid, P.xs, n, d, P.eps0, P.mx, &tile, s);
 
   // 6. retry loop (main.cu:312-430)
   uint32_t* list[2] = {(uint32_t*)w.list0.get(n * 4), (uint32_t*)w.list1.get(n * 4)};
@@ -714,6 +844,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   a.K = K;
   a.out_ids = d_ids;
   a.out_d = d_dists;
+  a.rowsum = rowsum;
   a.fail_count = &sm->fail_count;
   a.cand_count = &sm->cand;
   a.work_counter = &sm->work_counter;
@@ -778,8 +909,8 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     c.go = 0;
     if (dev_loop) write_small(w, dctl, &c, sizeof(LoopCtl), s);
     launch_zero_words(sm->chunk_fill, sizeof(sm->chunk_fill), s);
-    chunk_lists_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a.grid.pid, (uint32_t)n, crow, sm->chunk_fill,
-                                                                   clist);
+    chunk_lists_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a.grid.pid, nullptr, (uint32_t)n, crow,
+                                                                   sm->chunk_fill, clist);
     KNNSJ_CHECK_LAUNCH();
     launch_zero_words(&sm->fail_count, 4, s);
     launch_zero_words(&sm->fr, sizeof(FailRadii), s);
@@ -792,6 +923,8 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
       const uint64_t nr = std::min<uint64_t>(crow, n - r0);
       a.qlist = clist + r0;
       a.nq = (uint32_t)nr;
+      // (the queries of a block of ids are spread over the whole dataset:
+      // the per-query search, not query tiles)
       launch_search<T>(a, w.sm_count, s);
       KNNSJ_CUDA(cudaEventRecord(w.chunk_ev[ch], s));
       KNNSJ_CUDA(cudaStreamWaitEvent(w.copy_stream, w.chunk_ev[ch], 0));
@@ -941,7 +1074,10 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     launch_zero_words(&sm->fail_count, 4, s);
     launch_zero_words(&sm->fr, sizeof(FailRadii), s);
     rec(4);
-    launch_search<T>(a, w.sm_count, s);
+    if (iter == 0)
+      first_pass_search<T>(w, a, tile, sm, s);
+    else
+      launch_search<T>(a, w.sm_count, s);
     rec(5);
     struct {
       uint32_t fail;
@@ -990,9 +1126,14 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     w.mail = false;
     if (rows->checksum) read_small(w, &rows->total_distance, &sm->csum, sizeof(double), s);
   }
-  unsigned long long cand = 0;
+  if (rowsum && st) {
+    launch_sum_f64(rowsum, n, sm->cpart, &sm->csum, s);
+    read_small(w, &st->total_distance, &sm->csum, sizeof(double), s);
+  }
+  unsigned long long cand = 0, deferred = 0;
   uint32_t mlp_err = 0;
   read_small(w, &cand, &sm->cand, 8, s);
+  read_small(w, &deferred, &sm->defer_total, 8, s);
   if (qrad) read_small(w, &mlp_err, &sm->mlp_err, 4, s);
   if (mlp_err && cfg.verbose)  // rows are still exact: the affected queries started at eps0
     fprintf(stderr, "knnsj: the tensor-core radius model timed out (%u); those queries started at eps0\n", mlp_err);
@@ -1007,6 +1148,7 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
     st->search_alg_bytes = alg_bytes;
     st->search_alg_flops = 3.0 * d * (double)cand;
     st->radius_model_error = (double)mlp_err;
+    st->tile_handovers = (double)deferred;
     const float a01 = elapsed(0, 1), a12 = elapsed(1, 2);
     st->ms_prep = a01;
     st->ms_search = a12;
@@ -1060,10 +1202,10 @@ template void finish_row_stream<double>(Workspace&, const RowStream&, const int3
                                         cudaStream_t);
 
 template void run_join<float>(Workspace&, const JoinConfig&, const float*, const float*, uint64_t, uint32_t,
-                              uint32_t, int32_t*, float*, knnsj_stats*, cudaStream_t, RowStream*);
+                              uint32_t, int32_t*, float*, knnsj_stats*, cudaStream_t, RowStream*, double*);
 template void run_join<double>(Workspace&, const JoinConfig&, const double*, const double*, uint64_t,
                                uint32_t, uint32_t, int32_t*, double*, knnsj_stats*, cudaStream_t,
-                               RowStream*);
+                               RowStream*, double*);
 template void run_features<float>(Workspace&, const JoinConfig&, const float*, const float*, uint64_t, uint32_t,
                                   uint32_t, float*, double*, cudaStream_t);
 template void run_features<double>(Workspace&, const JoinConfig&, const double*, const double*, uint64_t,

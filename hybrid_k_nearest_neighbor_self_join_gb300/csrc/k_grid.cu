@@ -275,6 +275,55 @@ __global__ void gather_sorted_kernel(const T* __restrict__ soa, uint64_t n, uint
   }
 }
 
+// Morton (Z-order) code of a point's cell over the di indexed dimensions,
+// `bits` bits per dimension: bit b of cell coordinate j goes to bit b*di + j.
+template <typename T>
+__global__ void morton_key_kernel(const T* __restrict__ ps, uint64_t n, const GridGeom<T> g, int bits,
+                                  unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    unsigned long long code = 0;
+    for (uint32_t j = 0; j < g.di; j++) {
+      const uint32_t c = point_cell_coord(ps[(uint64_t)j * n + i], g.minv[j], g.width);
+      for (int b = 0; b < bits; b++) code |= (unsigned long long)((c >> b) & 1u) << (b * g.di + j);
+    }
+    keys[i] = code;
+    vals[i] = (uint32_t)i;
+  }
+}
+
+// Counting sort of points into the cells of a grid (any order within a
+// cell): tbl[L + 1] counts cell L, ...
+template <typename T>
+__global__ void cell_count_atomic_kernel(const T* __restrict__ xs, uint64_t n, const GridGeom<T> g,
+                                         uint32_t* __restrict__ tbl) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    unsigned long long lin = 0;
+    for (uint32_t j = 0; j < g.di; j++)
+      lin += (unsigned long long)point_cell_coord(xs[(uint64_t)j * n + i], g.minv[j], g.width) * g.mult[j];
+    atomicAdd(&tbl[lin + 1], 1u);
+  }
+}
+
+// ... after the exclusive scan tbl[L + 1] is the first position of cell L;
+// each point takes the next position of its cell (leaving tbl[L + 1] at the
+// cell's end, which is where cell L + 1 starts: tbl becomes the start table).
+template <typename T>
+__global__ void cell_scatter_atomic_kernel(const T* __restrict__ xs, uint64_t n, uint32_t d, const GridGeom<T> g,
+                                           uint32_t* __restrict__ tbl, T* __restrict__ ps,
+                                           uint32_t* __restrict__ pid) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    unsigned long long lin = 0;
+    for (uint32_t j = 0; j < g.di; j++)
+      lin += (unsigned long long)point_cell_coord(xs[(uint64_t)j * n + i], g.minv[j], g.width) * g.mult[j];
+    const uint32_t pos = atomicAdd(&tbl[lin + 1], 1u);
+    for (uint32_t j = 0; j < d; j++) ps[(uint64_t)j * n + pos] = xs[(uint64_t)j * n + i];
+    pid[pos] = (uint32_t)i;
+  }
+}
+
 unsigned grid_blocks(uint64_t n, int threads = 256) {
   uint64_t b = (n + threads - 1) / threads;
   if (b > 152ull * 64) b = 152ull * 64;
@@ -341,6 +390,24 @@ void launch_dense_table(const unsigned long long* ckeys, const uint32_t* coff, u
 }
 
 template <typename T>
+void launch_morton_keys(const T* ps, uint64_t n, const GridGeom<T>& g, int bits, unsigned long long* keys,
+                        uint32_t* vals, cudaStream_t s) {
+  morton_key_kernel<T><<<grid_blocks(n), 256, 0, s>>>(ps, n, g, bits, keys, vals);
+  KNNSJ_CHECK_LAUNCH();
+}
+
+template <typename T>
+void launch_counting_grid(const T* xs, uint64_t n, uint32_t d, const GridGeom<T>& g, uint32_t* tbl,
+                          uint32_t* scan_tmp, T* ps, uint32_t* pid, cudaStream_t s) {
+  launch_zero_words(tbl, (g.total_cells + 1) * 4, s);
+  cell_count_atomic_kernel<T><<<grid_blocks(n), 256, 0, s>>>(xs, n, g, tbl);
+  KNNSJ_CHECK_LAUNCH();
+  scan_exclusive_u32(tbl + 1, tbl + 1, g.total_cells, scan_tmp, s);
+  cell_scatter_atomic_kernel<T><<<grid_blocks(n), 256, 0, s>>>(xs, n, d, g, tbl, ps, pid);
+  KNNSJ_CHECK_LAUNCH();
+}
+
+template <typename T>
 void launch_gather_sorted(const T* soa, uint64_t n, uint32_t d, const uint32_t* sorted_ids, T* ps, float* psf,
                           cudaStream_t s) {
   gather_sorted_kernel<T><<<grid_blocks(n), 256, 0, s>>>(soa, n, d, sorted_ids, ps, psf);
@@ -351,6 +418,14 @@ template void launch_cell_ids<float>(const float*, uint64_t, const GridGeom<floa
                                      uint32_t*, cudaStream_t);
 template void launch_cell_ids<double>(const double*, uint64_t, const GridGeom<double>&, unsigned long long*,
                                       uint32_t*, cudaStream_t);
+template void launch_morton_keys<float>(const float*, uint64_t, const GridGeom<float>&, int, unsigned long long*,
+                                        uint32_t*, cudaStream_t);
+template void launch_morton_keys<double>(const double*, uint64_t, const GridGeom<double>&, int,
+                                         unsigned long long*, uint32_t*, cudaStream_t);
+template void launch_counting_grid<float>(const float*, uint64_t, uint32_t, const GridGeom<float>&, uint32_t*,
+                                          uint32_t*, float*, uint32_t*, cudaStream_t);
+template void launch_counting_grid<double>(const double*, uint64_t, uint32_t, const GridGeom<double>&, uint32_t*,
+                                           uint32_t*, double*, uint32_t*, cudaStream_t);
 template void launch_gather_sorted<float>(const float*, uint64_t, uint32_t, const uint32_t*, float*, float*,
                                           cudaStream_t);
 template void launch_gather_sorted<double>(const double*, uint64_t, uint32_t, const uint32_t*, double*, float*,

@@ -121,7 +121,32 @@ __global__ void checksum_final_kernel(const double* __restrict__ part, unsigned 
   *out = t;
 }
 
+// Sum of n doubles in a fixed order: grid-stride partial sums per thread,
+// warp butterflies, block partials summed in block order.
+__global__ void sum_f64_kernel(const double* __restrict__ v, uint64_t count, double* __restrict__ part) {
+  __shared__ double ws[32];
+  double s = 0.0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    s = __dadd_rn(s, v[i]);
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(FULL, s, off);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += ws[k];
+    part[blockIdx.x] = t;
+  }
+}
+
 }  // namespace
+
+void launch_sum_f64(const double* v, uint64_t count, double* d_partial, double* d_out, cudaStream_t s) {
+  sum_f64_kernel<<<CHECKSUM_BLOCKS, 256, 0, s>>>(v, count, d_partial);
+  KNNSJ_CHECK_LAUNCH();
+  checksum_final_kernel<<<1, 32, 0, s>>>(d_partial, CHECKSUM_BLOCKS, d_out);
+  KNNSJ_CHECK_LAUNCH();
+}
 
 template <typename T>
 void launch_checksum(const T* dists, uint64_t count, double* d_partial, double* d_out, cudaStream_t s) {

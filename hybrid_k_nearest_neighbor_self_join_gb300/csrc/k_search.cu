@@ -116,12 +116,14 @@ struct SearchParams {
   uint32_t qchunk;
   const uint32_t* __restrict__ qlist;
   uint32_t nq;
+  const uint32_t* nq_dev;  // non-null: the query count is read here
   const LoopCtl* ctl;
   T radius;
   T* qradius;
   double step;
   int32_t* out_ids;
   T* out_d;
+  double* rowsum;  // per-row verification sums (nullptr: none)
   uint32_t* fail_list;
   uint32_t* fail_count;
   unsigned long long* cand_count;
@@ -331,7 +333,8 @@ __device__ KNNSJ_REDUCE_LINKAGE Sel<T> reduce(typename Key<T>::type* buf, uint32
 template <typename T>
 __device__ KNNSJ_WRITE_LINKAGE void write_sorted_row(typename Key<T>::type* buf, uint32_t* cnt, uint32_t len,
                                               typename Key<T>::type top, uint32_t K, int32_t* __restrict__ out_ids,
-                                              T* __restrict__ out_d, uint64_t row_out, int lane) {
+                                              T* __restrict__ out_d, uint64_t row_out, int lane,
+                                              double* __restrict__ rowsum) {
   using Kt = Key<T>;
   using KT = typename Kt::type;
   constexpr int R = HIST_MAX_B / 32;
@@ -414,6 +417,7 @@ __device__ KNNSJ_WRITE_LINKAGE void write_sorted_row(typename Key<T>::type* buf,
     for (int off = 16; off > 0; off >>= 1) e = max(e, __shfl_xor_sync(FULL, e, off));
     end = e ? e : len;
   }
+  T rsq = 0;
   for (uint32_t p0 = 0; p0 < end; p0 += 32) {
     const uint32_t pp = p0 + lane;
     if (pp < end) {
@@ -426,11 +430,14 @@ __device__ KNNSJ_WRITE_LINKAGE void write_sorted_row(typename Key<T>::type* buf,
         for (uint32_t j = first; j < last; j++) rank += Kt::less(buf[j], w) ? 1u : 0u;
       const uint32_t fin = first + rank;
       if (fin < K) {
+        const T dist = Num<T>::sqrt(Kt::acc(w));
         out_ids[row_out + fin] = (int32_t)Kt::id(w);
-        out_d[row_out + fin] = Num<T>::sqrt(Kt::acc(w));
+        out_d[row_out + fin] = dist;
+        rsq = Num<T>::add(rsq, Num<T>::mul(dist, dist));
       }
     }
   }
+  if (rowsum) store_row_sum<T>(rowsum, row_out / K, rsq, lane);
   __syncwarp();
 }
 
@@ -438,36 +445,23 @@ __device__ KNNSJ_WRITE_LINKAGE void write_sorted_row(typename Key<T>::type* buf,
 template <typename T>
 __device__ __noinline__ void write_sorted_row_bitonic(typename Key<T>::type* buf, uint32_t len, uint32_t K,
                                                       int32_t* __restrict__ out_ids, T* __restrict__ out_d,
-                                                      uint64_t row_out, int lane) {
+                                                      uint64_t row_out, int lane, double* __restrict__ rowsum) {
   using Kt = Key<T>;
   const uint32_t n2 = len <= 1 ? 1u : (1u << (32 - __clz(len - 1)));
   __syncwarp();
   for (uint32_t i = len + lane; i < n2; i += 32) buf[i] = Kt::maxv();
   __syncwarp();
   warp_bitonic_sort<T>(buf, (int)n2, lane);
+  T rsq = 0;
   for (uint32_t i = lane; i < K; i += 32) {
     const typename Kt::type kk = buf[i];
+    const T dist = Num<T>::sqrt(Kt::acc(kk));
     out_ids[row_out + i] = (int32_t)Kt::id(kk);
-    out_d[row_out + i] = Num<T>::sqrt(Kt::acc(kk));
+    out_d[row_out + i] = dist;
+    rsq = Num<T>::add(rsq, Num<T>::mul(dist, dist));
   }
+  if (rowsum) store_row_sum<T>(rowsum, row_out / K, rsq, lane);
   __syncwarp();
-}
-
-// A lower (up = false) or upper (up = true) bound of the grid cell of
-// coordinate v, clamped to [0, ncell-1], from float arithmetic with a
-// reciprocal: (v - minf) * invw is within 2^-22 relative of (v - min) / width
-// (the rounding of v - minf, of 1/width, of the product, and of min and
-// width to float), plus 2^-24 |minf| * invw from rounding min; the bound
-// moves by twice that, so the true cell of any coordinate on the far side
-// of v (the grid's own monotone division in the data type) is never cut off.
-__device__ __forceinline__ uint32_t ring_cell(float v, float minf, float invw, uint32_t ncell, bool up) {
-  const float u = (v - minf) * invw;
-  const float tol = (fabsf(u) + fabsf(minf) * invw) * (1.0f / 2097152.0f) + (1.0f / 1048576.0f);
-  const float ub = up ? u + tol : u - tol;
-  if (!(ub > 0.0f)) return 0;
-  if (!(ub < (float)ncell)) return ncell - 1;
-  const uint32_t c = (uint32_t)ub;
-  return c < ncell ? c : ncell - 1;
 }
 
 // Bitonic sort of one 64-bit value per lane across the warp (ascending).
@@ -543,7 +537,7 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
       s_fail = p.ctl->list[p.ctl->cur ^ 1];
       s_radius = (T)p.ctl->r;
     } else {
-      s_nq = p.nq;
+      s_nq = p.nq_dev ? *p.nq_dev : p.nq;
       s_qlist = p.qlist;
       s_fail = p.fail_list;
       s_radius = p.radius;
@@ -910,9 +904,9 @@ __global__ void __launch_bounds__(SEARCH_THREADS, search_min_blocks<T, D, DI>())
 #if KNNSJ_PRE_WRITE_REDUCE
           if (st.len > 2 * K && st.len > 64) st = reduce<T>(buf, hist, st, K, B, lane);
 #endif
-          write_sorted_row<T>(buf, hist, st.len, st.tau, K, p.out_ids, p.out_d, row_out, lane);
+          write_sorted_row<T>(buf, hist, st.len, st.tau, K, p.out_ids, p.out_d, row_out, lane, p.rowsum);
         } else {
-          write_sorted_row_bitonic<T>(buf, st.len, K, p.out_ids, p.out_d, row_out, lane);
+          write_sorted_row_bitonic<T>(buf, st.len, K, p.out_ids, p.out_d, row_out, lane, p.rowsum);
         }
       } else if (lane == 0) {
         const uint32_t slot = atomicAdd(p.fail_count, 1u);
@@ -963,7 +957,7 @@ void launch_one(const SearchParams<T>& prm, int wpb_req, int sm_count, cudaStrea
   const uint64_t need_blocks = (warps_needed + wpb - 1) / wpb;
   // inside the retry graph the pass size is known only on the device: the
   // full persistent grid, whose surplus warps find no work and leave
-  if (!prm.ctl && need_blocks < blocks) blocks = need_blocks;
+  if (!prm.ctl && !prm.nq_dev && need_blocks < blocks) blocks = need_blocks;
   if (blocks < 1) blocks = 1;
   kern<<<(unsigned)blocks, wpb * 32, smem, s>>>(prm);
   KNNSJ_CHECK_LAUNCH();
@@ -1042,7 +1036,7 @@ __global__ void __launch_bounds__(BRUTE_THREADS) brute_kernel(const SearchParams
       }
     }
   }
-  write_sorted_row_bitonic<T>(buf, st.len, K, p.out_ids, p.out_d, (uint64_t)qid * K, lane);
+  write_sorted_row_bitonic<T>(buf, st.len, K, p.out_ids, p.out_d, (uint64_t)qid * K, lane, p.rowsum);
 }
 
 }  // namespace
@@ -1062,6 +1056,7 @@ void launch_brute(const SearchLaunch<T>& a, cudaStream_t s) {
   p.nq = a.nq;
   p.out_ids = a.out_ids;
   p.out_d = a.out_d;
+  p.rowsum = a.rowsum;
   const size_t per_warp = (size_t)p.B * sizeof(typename Key<T>::type) + 256 * 4;
   int wpb = BRUTE_THREADS / 32;
   while (wpb > 1 && per_warp * wpb + a.d * sizeof(T) > 200 * 1024) wpb--;
@@ -1107,12 +1102,14 @@ void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s) {
   const int wpb = a.shape.warps_per_block;
   p.qlist = a.qlist;
   p.nq = a.nq;
+  p.nq_dev = a.nq_dev;
   p.ctl = a.ctl;
   p.radius = a.radius;
   p.qradius = a.qradius;
   p.step = (double)a.step;
   p.out_ids = a.out_ids;
   p.out_d = a.out_d;
+  p.rowsum = a.rowsum;
   p.fail_list = a.fail_list;
   p.fail_count = a.fail_count;
   p.cand_count = a.cand_count;

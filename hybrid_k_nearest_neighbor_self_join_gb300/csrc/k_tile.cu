@@ -1,0 +1,622 @@
+// k_tile.cu -- range search of low-dimensional float data by tiles of
+// queries: one warp owns up to 32 queries that are neighbours in cell order,
+// one lane per query, and the tile's queries share one pass over the
+// candidates of the union of their cell rings.
+//
+// Replaces, for the first search pass of float data with two or three
+// dimensions (all indexed) and k+1 <= 65, the same reference steps as
+// search_kernel (k_search.cu): kernelNDGridIndexGlobalkNN with evaluateCell
+// and evalPoint (kernel.cu:61-225), the pair buffer and the two
+// thrust::stable_sort_by_key (GPU.cu:1629-1634), and the K-row extraction of
+// storeNeighborTableForkNNOnTheFly (GPU.cu:3610-3704).
+//
+// Per tile (one warp):
+//   1. every lane computes its query's cell ring, the warp takes the union
+//      box (lanes whose ring is much wider than the tile's median are handed
+//      to search_kernel instead, so one outlier does not widen everyone's
+//      scan); each ring row of the box (consecutive cells along dimension 0)
+//      is one contiguous run of the cell-ordered columns;
+//   2. candidates are staged in shared memory 128 at a time (coalesced
+//      loads: coordinates and id in one 16-byte record) and read back by every
+//      lane at once (broadcast);
+//   3. pass 1: each lane counts its candidates within its own radius in 32
+//      bins of squared distance (a monotone map of [0, r^2]): the bin holding
+//      the K-th smallest, the count below it, and whether the query can be
+//      accepted (at least K points within r, the reference's rule,
+//      GPU.cu:3659-3669);
+//      when the boundary bin holds more keys than the overflow area, a
+//      refinement pass splits that bin 32 ways (at most two refinements;
+//      beyond, the query goes to search_kernel: only exact ties get there);
+//   4. pass 2: keys below the boundary bin are placed at their bin's running
+//      position in the lane's row (a counting sort by bin), keys of the
+//      boundary bin go to a small per-lane overflow list;
+//   5. each lane insertion-sorts its row (bins are already in order, so this
+//      only orders keys within a bin), sorts the overflow list and completes
+//      the row with its smallest keys; the warp then writes the 32 rows with
+//      coalesced stores, distances as sqrt in the data type.
+// Squared distances use the reference's fma chain in dimension order
+// (kernel.cu:139-140) exactly as search_kernel does, so rows are identical.
+// Keys are (squared distance bits, id) in one u64: ties are ordered by id.
+
+#include <cmath>
+#include <cstdlib>
+
+#include "knnsj_internal.h"
+
+namespace knnsj {
+
+namespace {
+
+constexpr int TILE_WARPS = 4;                    // warps per block
+constexpr int TILE_THREADS = TILE_WARPS * 32;
+constexpr int TILE_CH = 128;                     // staged candidates per chunk
+constexpr int TILE_BINS = 32;
+constexpr int TILE_OV = 16;                      // overflow keys per lane
+constexpr int TILE_OV_PITCH = TILE_OV + 1;       // u64 words per lane (odd: spreads banks)
+constexpr uint32_t TILE_MAX_ROWS = 4096;         // larger union boxes go to search_kernel
+
+struct alignas(16) Cand {
+  float x[3];
+  uint32_t id;
+};
+
+// shared memory of one warp (bytes): QPT queries with rows of up to KMAX
+// keys.  Pitches are odd (rows, overflow lists in u64 words; histograms in
+// u32 words), so queries at the same index fall in different banks.
+template <int QPT, int KMAX>
+struct TileSmem {
+  static constexpr int KP = (KMAX % 2 == 1) ? KMAX : KMAX + 1;
+  static constexpr int HP = TILE_BINS + 1;
+  static constexpr int CAND = 0;
+  static constexpr int HIST = CAND + TILE_CH * 16;           // [QPT][HP] u32
+  static constexpr int AUX = HIST + QPT * HP * 4;             // [QPT][HP] u32 (refinement)
+  static constexpr int OVC = AUX + QPT * HP * 4;              // [QPT] u32 overflow counts
+  static constexpr int OV = (OVC + QPT * 4 + 7) / 8 * 8;      // [QPT][TILE_OV_PITCH] u64
+  static constexpr int ROWS = OV + QPT * TILE_OV_PITCH * 8;   // [QPT][KP] u64
+  static constexpr int RUNS = ROWS + QPT * KP * 8;            // 2 x 32 u32
+  static constexpr int BYTES = RUNS + 2 * 32 * 4;
+};
+
+struct TileParams {
+  GridGeom<float> g;                    // candidate grid
+  const float* __restrict__ ps;         // candidate columns in cell order (d x n)
+  const uint32_t* __restrict__ pid;     // original id of each cell-ordered position
+  const uint32_t* __restrict__ dstart;  // first position of every linear cell id (dense table)
+  uint64_t n;
+  uint32_t K;
+  const float* __restrict__ qps;        // query columns: cell order (qlist null) or input order
+  const uint32_t* __restrict__ qpid;    // ids of qps positions (qlist null)
+  const uint32_t* __restrict__ qlist;   // query ids, or null: the positions of qps in qorder
+  const uint32_t* __restrict__ qorder;  // positions of qps in tile order (null: 0, 1, ...)
+  uint32_t nq;
+  float radius;                         // uniform radius (qradius null)
+  float* qradius;                       // per-query radius by id
+  double step;                          // least growth of a failed per-query radius
+  int32_t* out_ids;
+  float* out_d;
+  double* rowsum;                       // per-row verification sums (null: none)
+  uint32_t* fail_list;
+  uint32_t* fail_count;
+  uint32_t* defer_list;                 // queries handed to search_kernel at the same radius
+  uint32_t* defer_count;
+  unsigned long long* cand_count;
+  uint32_t* work_counter;
+  FailRadii* fail_radii;
+};
+
+// round(a * s + c) clamped to [0, 31], with the integer read from the low
+// mantissa bits of a + 1.5 * 2^23 (one FMA); monotone in a.  c must be an
+// integer (exact in float).
+__device__ __forceinline__ int tbin(float a, float s, float cm) {
+  const int v = __float_as_int(__fmaf_rn(a, s, cm)) - 0x4b400000;
+  return min(max(v, 0), TILE_BINS - 1);
+}
+
+// Warp-aggregated append of this lane's value to a global list.
+__device__ __forceinline__ void warp_append(bool want, uint32_t v, uint32_t* list, uint32_t* count, int lane) {
+  const unsigned m = __ballot_sync(FULL, want);
+  if (!m) return;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+  base = __shfl_sync(FULL, base, leader);
+  if (want) list[base + __popc(m & lanemask_lt())] = v;
+}
+
+// QPT queries per warp (8, 16 or 32), LPQ = 32 / QPT lanes per query: lane
+// (slot qs = lane % QPT, phase ph = lane / QPT) evaluates the staged
+// candidates ph, ph + LPQ, ... for query qs.  The query's lanes share its
+// histogram, row and overflow list through shared-memory atomics; the lane
+// of phase 0 does the query's serial steps.
+template <int D, int KMAX, int QPT>
+__global__ void __launch_bounds__(TILE_THREADS, 4) tile_kernel(const TileParams p) {
+  using SM = TileSmem<QPT, KMAX>;
+  constexpr int LPQ = 32 / QPT;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int qs = lane % QPT;
+  const int ph = lane / QPT;
+  const bool lead = ph == 0;
+  unsigned char* ws = smem + (size_t)wib * SM::BYTES;
+  Cand* cand = reinterpret_cast<Cand*>(ws + SM::CAND);
+  uint32_t* hq = reinterpret_cast<uint32_t*>(ws + SM::HIST) + qs * SM::HP;  // this query's bins
+  uint32_t* aq = reinterpret_cast<uint32_t*>(ws + SM::AUX) + qs * SM::HP;
+  uint32_t* ovc = reinterpret_cast<uint32_t*>(ws + SM::OVC) + qs;
+  unsigned long long* myov = reinterpret_cast<unsigned long long*>(ws + SM::OV) + (size_t)qs * TILE_OV_PITCH;
+  unsigned long long* rows = reinterpret_cast<unsigned long long*>(ws + SM::ROWS);  // [QPT][KP]
+  unsigned long long* myrow = rows + (size_t)qs * SM::KP;
+  uint32_t* runS = reinterpret_cast<uint32_t*>(ws + SM::RUNS);
+  uint32_t* runP = runS + 32;
+
+  __shared__ float s_minf[3];
+  __shared__ float s_invw;
+  if (threadIdx.x < 3) s_minf[threadIdx.x] = threadIdx.x < (unsigned)D ? (float)p.g.minv[threadIdx.x] : 0.0f;
+  if (threadIdx.x == 0) s_invw = 1.0f / (float)p.g.width;
+  __syncthreads();
+
+  const uint64_t n = p.n;
+  const uint32_t K = p.K;
+  const uint32_t ntiles = (p.nq + QPT - 1) / QPT;
+  unsigned long long scanned = 0;
+
+  for (;;) {
+    uint32_t t = 0;
+    if (lane == 0) t = atomicAdd(p.work_counter, 1u);
+    t = __shfl_sync(FULL, t, 0);
+    if (t >= ntiles) break;
+    const uint32_t qi = t * (uint32_t)QPT + (uint32_t)qs;
+    const bool valid = qi < p.nq;
+    uint32_t qid = 0;
+    float q[D];
+    float r = 0.0f;
+#pragma unroll
+    for (int j = 0; j < D; j++) q[j] = 0.0f;
+    if (valid) {
+      const uint32_t pos = p.qorder ? p.qorder[qi] : qi;
+      qid = p.qlist ? p.qlist[qi] : p.qpid[pos];
+      const uint64_t col = p.qlist ? (uint64_t)qid : (uint64_t)pos;
+#pragma unroll
+      for (int j = 0; j < D; j++) q[j] = p.qps[(uint64_t)j * n + col];
+      r = p.qradius ? p.qradius[qid] : p.radius;
+    }
+
+    // 1. the query's ring (as search_kernel computes it) and the union box
+    const float rf = r * (1.0f + 1.0f / 8192.0f);
+    uint32_t lo[D], hi[D];
+    uint32_t ext = 0;
+#pragma unroll
+    for (int j = 0; j < D; j++) {
+      const float slack = (fabsf(q[j]) + rf) * (1.0f / 2097152.0f);
+      lo[j] = ring_cell(q[j] - rf - slack, s_minf[j], s_invw, p.g.ncell[j], false);
+      hi[j] = ring_cell(q[j] + rf + slack, s_minf[j], s_invw, p.g.ncell[j], true);
+      ext = max(ext, hi[j] - lo[j] + 1);
+    }
+    // queries whose ring is far wider than the tile's median go to search_kernel
+    bool defer = false;
+    {
+      const uint32_t e = valid ? ext : 0xffffffffu;
+      unsigned long long key = ((unsigned long long)e << 32) | (unsigned)lane;
+#pragma unroll
+      for (int kk = 2; kk <= 32; kk <<= 1) {
+#pragma unroll
+        for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+          const unsigned long long o = __shfl_xor_sync(FULL, key, jj);
+          const bool up = (lane & kk) == 0;
+          const bool low = (lane & jj) == 0;
+          const unsigned long long mn = key < o ? key : o;
+          const unsigned long long mx = key < o ? o : key;
+          key = (low == up) ? mn : mx;
+        }
+      }
+      const int nvalid = __popc(__ballot_sync(FULL, valid));  // (each query counted LPQ times)
+      const uint32_t med = (uint32_t)(__shfl_sync(FULL, key, (nvalid - 1) >> 1) >> 32);
+      defer = valid && ext > 2u * med + 2u;
+    }
+    bool in = valid && !defer;  // queries searched by this tile
+    uint32_t LO[D], HI[D];
+#pragma unroll
+    for (int j = 0; j < D; j++) {
+      LO[j] = __reduce_min_sync(FULL, in ? lo[j] : 0xffffffffu);
+      HI[j] = __reduce_max_sync(FULL, in ? hi[j] : 0u);
+    }
+    const uint32_t ext1 = HI[1] - LO[1] + 1;
+    const uint32_t ext2 = D == 3 ? HI[D - 1] - LO[D - 1] + 1 : 1u;
+    uint64_t nrows64 = __ballot_sync(FULL, in) ? (uint64_t)ext1 * ext2 : 0;
+    if (nrows64 > TILE_MAX_ROWS) {  // (uniform) the whole tile goes to search_kernel
+      defer = valid;
+      in = false;
+      nrows64 = 0;
+    }
+    const uint32_t nrows = (uint32_t)nrows64;
+    warp_append(defer && lead, qid, p.defer_list, p.defer_count, lane);
+
+    const float thr = in ? within_threshold(r) : -1.0f;  // acc <= thr never holds off the tile
+    const float s0 = (thr > 0.0f && thr < 3.0e38f) ? __fdividef((float)TILE_BINS, thr) : 0.0f;
+    const float MAG = 12582912.0f;  // 1.5 * 2^23
+
+    // Visits every candidate of the union box; body(c, live) runs on every
+    // lane, live when c is a candidate of this lane's phase.
+    auto for_each_candidate = [&](auto&& body) -> uint32_t {
+      uint32_t visited = 0;
+      for (uint32_t g0 = 0; g0 < nrows; g0 += 32) {
+        const uint32_t ridx = g0 + (uint32_t)lane;
+        uint32_t rs = 0, len = 0;
+        if (ridx < nrows) {
+          unsigned long long rbase;
+          if constexpr (D == 2) {
+            rbase = (unsigned long long)(LO[1] + ridx) * p.g.mult[1];
+          } else {
+            const uint32_t a1 = ridx % ext1, a2 = ridx / ext1;
+            rbase = (unsigned long long)(LO[1] + a1) * p.g.mult[1] + (unsigned long long)(LO[D - 1] + a2) * p.g.mult[D - 1];
+          }
+          rs = p.dstart[rbase + LO[0]];
+          len = p.dstart[rbase + HI[0] + 1] - rs;
+        }
+        uint32_t incl = len;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const uint32_t tt = __shfl_up_sync(FULL, incl, off);
+          if (lane >= off) incl += tt;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        visited += total;
+        __syncwarp();
+        runS[lane] = rs;
+        runP[lane] = incl - len;
+        __syncwarp();
+        // chunks are loaded one ahead: the loads of chunk c + 1 are in flight
+        // while chunk c is evaluated
+        int row = 0;
+        Cand pre[TILE_CH / 32];
+        auto fetch = [&](uint32_t c0) {
+#pragma unroll
+          for (int m = 0; m < TILE_CH / 32; m++) {
+            const uint32_t v = c0 + (uint32_t)(m * 32 + lane);
+            if (v < total) {
+              while (row < 31 && runP[row + 1] <= v) row++;
+              const uint32_t pos = runS[row] + (v - runP[row]);
+#pragma unroll
+              for (int j = 0; j < 3; j++) pre[m].x[j] = j < D ? p.ps[(uint64_t)j * n + pos] : 0.0f;
+              pre[m].id = p.pid[pos];
+            }
+          }
+        };
+        if (total) fetch(0);
+        for (uint32_t c0 = 0; c0 < total; c0 += TILE_CH) {
+          const uint32_t cnt = min((uint32_t)TILE_CH, total - c0);
+          __syncwarp();
+#pragma unroll
+          for (int m = 0; m < TILE_CH / 32; m++)
+            if (c0 + (uint32_t)(m * 32 + lane) < total) cand[m * 32 + lane] = pre[m];
+          __syncwarp();
+          if (c0 + TILE_CH < total) fetch(c0 + TILE_CH);
+          const uint32_t steps = (cnt + LPQ - 1) / LPQ;
+          uint32_t st = 0;
+          for (; st + 4 <= steps; st += 4) {
+            Cand c4[4];
+            bool l4[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+              const uint32_t j = (st + u) * LPQ + ph;
+              l4[u] = j < cnt;
+              c4[u] = cand[l4[u] ? j : 0];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) body(c4[u], l4[u]);
+          }
+          for (; st < steps; st++) {
+            const uint32_t j = st * LPQ + ph;
+            const bool live = j < cnt;
+            const Cand cc = cand[live ? j : 0];
+            body(cc, live);
+          }
+        }
+        __syncwarp();
+      }
+      return visited;
+    };
+    auto sqdist = [&](const Cand& c) -> float {
+      float acc = 0.0f;
+#pragma unroll
+      for (int j = 0; j < D; j++) {
+        const float tt = __fsub_rn(c.x[j], q[j]);
+        acc = __fmaf_rn(tt, tt, acc);
+      }
+      return acc;
+    };
+    // zeroes a query's 32 bins (its LPQ lanes share the work)
+    auto clear_bins = [&](uint32_t* h) {
+      for (int b = ph; b < TILE_BINS; b += LPQ) h[b] = 0u;
+    };
+
+    // 3. pass 1: counts per bin of squared distance within the radius
+    clear_bins(hq);
+    __syncwarp();
+    const uint32_t box_points = for_each_candidate([&](const Cand& c, bool live) {
+      const float acc = sqdist(c);
+      if (live && acc <= thr) atomicAdd(&hq[tbin(acc, s0, MAG)], 1u);
+    });
+    // candidates evaluated: the union box's points for every query it serves
+    scanned += (unsigned long long)box_points * (unsigned)__popc(__ballot_sync(FULL, in && lead));
+    __syncwarp();
+    // boundary bin of level 0 and the counts below it (the query's lead lane);
+    // its bins become the exclusive prefix
+    uint32_t found = 0, c_lo = 0, m = 0, bs0 = TILE_BINS;
+    if (lead) {
+      uint32_t cum = 0;
+      for (int b = 0; b < TILE_BINS; b++) {
+        const uint32_t h = hq[b];
+        hq[b] = cum;
+        if (bs0 == TILE_BINS && cum + h >= K) {
+          bs0 = (uint32_t)b;
+          c_lo = cum;
+          m = h;
+        }
+        cum += h;
+      }
+      found = cum;
+    }
+    found = __shfl_sync(FULL, found, qs);
+    c_lo = __shfl_sync(FULL, c_lo, qs);
+    m = __shfl_sync(FULL, m, qs);
+    bs0 = __shfl_sync(FULL, bs0, qs);
+    bool ok = in && found >= K;
+    // refinement of the boundary bin while it overflows the overflow list
+    int lev = 0;
+    int bs[3] = {(int)bs0, TILE_BINS, TILE_BINS};
+    float sl[3] = {s0, 0.0f, 0.0f}, cl[3] = {0.0f, 0.0f, 0.0f};  // scale and integer offset per level
+#pragma unroll
+    for (int L = 1; L < 3; L++) {
+      const bool need = ok && lev == L - 1 && m > (uint32_t)TILE_OV;
+      if (!__any_sync(FULL, need)) break;
+      if (need) {
+        sl[L] = sl[L - 1] * (float)TILE_BINS;
+        cl[L] = (float)TILE_BINS * (cl[L - 1] - ((float)bs[L - 1] - 0.5f));
+        clear_bins(aq);
+      }
+      __syncwarp();
+      for_each_candidate([&](const Cand& c, bool live) {
+        const float acc = sqdist(c);
+        if (live && need && acc <= thr && tbin(acc, sl[0], MAG) == bs[0]) {
+          bool member = true;
+#pragma unroll
+          for (int l2 = 1; l2 < L; l2++)
+            if (tbin(acc, sl[l2], MAG + cl[l2]) != bs[l2]) member = false;
+          if (member) atomicAdd(&aq[tbin(acc, sl[L], MAG + cl[L])], 1u);
+        }
+      });
+      __syncwarp();
+      uint32_t nb = TILE_BINS, nlo = c_lo, nm = m;
+      if (need && lead) {
+        uint32_t cum = c_lo;
+        for (int b = 0; b < TILE_BINS; b++) {
+          const uint32_t h = aq[b];
+          if (nb == TILE_BINS && cum + h >= K) {
+            nb = (uint32_t)b;
+            nlo = cum;
+            nm = h;
+          }
+          cum += h;
+        }
+      }
+      nb = __shfl_sync(FULL, nb, qs);
+      nlo = __shfl_sync(FULL, nlo, qs);
+      nm = __shfl_sync(FULL, nm, qs);
+      if (need) {
+        bs[L] = (int)nb;
+        c_lo = nlo;
+        m = nm;
+        lev = L;
+      }
+      __syncwarp();
+    }
+    // still more boundary keys than the overflow list holds (exact ties):
+    // search_kernel takes the query
+    const bool tie_defer = ok && m > (uint32_t)TILE_OV;
+    warp_append(tie_defer && lead, qid, p.defer_list, p.defer_count, lane);
+    ok = ok && !tie_defer;
+
+    // 4. pass 2: keys below the boundary bin to their bin's running slot,
+    // keys of the boundary bin to the overflow list
+    if (lead) *ovc = 0u;
+    __syncwarp();
+    if (__any_sync(FULL, ok)) {
+      for_each_candidate([&](const Cand& c, bool live) {
+        const float acc = sqdist(c);
+        if (live && ok && acc <= thr) {
+          const int b0 = tbin(acc, sl[0], MAG);
+          int slot_bin = -1;
+          bool over = false;
+          if (b0 < bs[0]) {
+            slot_bin = b0;
+          } else if (b0 == bs[0]) {
+            if (lev == 0) {
+              over = true;
+            } else {
+              const int b1 = tbin(acc, sl[1], MAG + cl[1]);
+              if (b1 < bs[1]) {
+                slot_bin = b0;
+              } else if (b1 == bs[1]) {
+                if (lev == 1) {
+                  over = true;
+                } else {
+                  const int b2 = tbin(acc, sl[2], MAG + cl[2]);
+                  if (b2 < bs[2])
+                    slot_bin = b0;
+                  else if (b2 == bs[2])
+                    over = true;
+                }
+              }
+            }
+          }
+          const unsigned long long key = ((unsigned long long)__float_as_uint(acc) << 32) | c.id;
+          if (slot_bin >= 0) myrow[atomicAdd(&hq[slot_bin], 1u)] = key;
+          if (over) myov[atomicAdd(ovc, 1u)] = key;
+        }
+      });
+    }
+    __syncwarp();
+
+    // 5. rows in order: insertion sort (keys are already grouped by bin);
+    // the overflow list is sorted by a second lane of the query when there
+    // is one, and its smallest keys complete the row
+    const bool sorter_row = ok && lead;
+    const bool sorter_ov = ok && (LPQ > 1 ? ph == 1 : lead);
+    const uint32_t nov = *ovc;
+    if (sorter_row) {
+      for (uint32_t i = 1; i < c_lo; i++) {
+        const unsigned long long key = myrow[i];
+        uint32_t j = i;
+        while (j > 0) {
+          const unsigned long long prev = myrow[j - 1];
+          if (prev <= key) break;
+          myrow[j] = prev;
+          j--;
+        }
+        myrow[j] = key;
+      }
+    }
+    if (sorter_ov) {
+      for (uint32_t i = 1; i < nov; i++) {
+        const unsigned long long key = myov[i];
+        uint32_t j = i;
+        while (j > 0) {
+          const unsigned long long prev = myov[j - 1];
+          if (prev <= key) break;
+          myov[j] = prev;
+          j--;
+        }
+        myov[j] = key;
+      }
+    }
+    __syncwarp();
+    if (sorter_row)
+      for (uint32_t i = c_lo; i < K; i++) myrow[i] = myov[i - c_lo];
+    __syncwarp();
+    // coalesced row writes: the warp writes each accepted query's row
+    {
+      unsigned mask = __ballot_sync(FULL, ok && lead);
+      while (mask) {
+        const int rl = __ffs(mask) - 1;  // (a lead lane: its index is the query slot)
+        mask &= mask - 1;
+        const uint32_t rid = __shfl_sync(FULL, qid, rl);
+        const unsigned long long* src = rows + (size_t)rl * SM::KP;
+        const uint64_t base = (uint64_t)rid * K;
+        float rsq = 0.0f;
+        for (uint32_t s = (uint32_t)lane; s < K; s += 32) {
+          const unsigned long long key = src[s];
+          const float dist = __fsqrt_rn(__uint_as_float((uint32_t)(key >> 32)));
+          p.out_ids[base + s] = (int32_t)(uint32_t)key;
+          p.out_d[base + s] = dist;
+          rsq = __fadd_rn(rsq, __fmul_rn(dist, dist));
+        }
+        if (p.rowsum) store_row_sum<float>(p.rowsum, rid, rsq, lane);
+      }
+    }
+    // failures: fewer than K points within the radius
+    const bool fail = in && found < K;
+    warp_append(fail && lead, qid, p.fail_list, p.fail_count, lane);
+    if (fail && lead && p.qradius) {
+      // per-query radii grow by at least eps0/2, toward K points from the
+      // count found within the radius: (K / found)^(1/dims), at most 4x
+      double rn = (double)r + p.step;
+      const float f = exp2f(log2f((float)K / (float)max(found, 1u)) / (float)D) * 1.05f;
+      rn = fmax(rn, (double)r * (double)fminf(fmaxf(f, 1.0f), 4.0f));
+      const float rt = (float)rn;
+      p.qradius[qid] = rt;
+      atomicMax(&p.fail_radii->rmax_bits, (unsigned long long)__float_as_uint(rt));
+      const float oct = log2f(rt / (2.0f * (float)p.step));  // log2(r / eps0)
+      const int bin = min(max((int)floorf(4.0f * oct) + 16, 0), FAIL_RADIUS_BINS - 1);
+      atomicAdd(&p.fail_radii->hist[bin], 1u);
+    }
+    __syncwarp();
+  }
+  if (lane == 0 && scanned) atomicAdd(p.cand_count, scanned);
+}
+
+template <int D, int KMAX, int QPT>
+void launch_tile_kernel(const TileParams& prm, int sm_count, cudaStream_t s) {
+  using SM = TileSmem<QPT, KMAX>;
+  const size_t smem = (size_t)SM::BYTES * TILE_WARPS;
+  auto kern = tile_kernel<D, KMAX, QPT>;
+  KNNSJ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  KNNSJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TILE_THREADS, smem));
+  if (per_sm < 1) throw StatusError{KNNSJ_ERR_UNSUPPORTED, "tile kernel does not fit"};
+  const uint64_t tiles = ((uint64_t)prm.nq + QPT - 1) / QPT;
+  uint64_t blocks = (uint64_t)per_sm * sm_count;
+  const uint64_t need = (tiles + TILE_WARPS - 1) / TILE_WARPS;
+  if (need < blocks) blocks = need;
+  if (blocks < 1) blocks = 1;
+  kern<<<(unsigned)blocks, TILE_THREADS, smem, s>>>(prm);
+  KNNSJ_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+bool tile_search_applies(uint32_t d, uint32_t di, uint32_t K, int dense, size_t elem) {
+  return elem == 4 && (d == 2 || d == 3) && di == d && K <= 65 && dense;
+}
+
+template <typename T>
+void launch_tile_search(const SearchLaunch<T>& a, uint32_t* defer_list, uint32_t* defer_count, int sm_count,
+                        cudaStream_t s) {
+  if constexpr (sizeof(T) != 4) {
+    throw StatusError{KNNSJ_ERR_UNSUPPORTED, "tile search is float only"};
+  } else {
+    if (a.nq == 0) return;
+    TileParams p{};
+    p.g = a.grid.geom;
+    p.ps = a.grid.ps;
+    p.pid = a.grid.pid;
+    p.dstart = a.grid.dstart;
+    p.n = a.n;
+    p.K = a.K;
+    p.qlist = a.qlist;
+    p.qps = a.qlist ? a.xs : (a.qps ? a.qps : a.grid.ps);
+    p.qpid = a.qps ? a.qpid : a.grid.pid;
+    p.qorder = a.qlist ? nullptr : a.qorder;
+    p.nq = a.nq;
+    p.radius = a.radius;
+    p.qradius = a.qradius;
+    p.step = (double)a.step;
+    p.out_ids = a.out_ids;
+    p.out_d = a.out_d;
+    p.rowsum = a.rowsum;
+    p.fail_list = a.fail_list;
+    p.fail_count = a.fail_count;
+    p.defer_list = defer_list;
+    p.defer_count = defer_count;
+    p.cand_count = a.cand_count;
+    p.work_counter = a.work_counter;
+    p.fail_radii = a.fail_radii;
+    launch_zero_words(a.work_counter, sizeof(uint32_t), s);
+    const bool d3 = a.d == 3;
+    // queries per tile: fewer queries per tile widen the union box less (a
+    // tile's queries cover a smaller share of one query's neighbourhood)
+    int qpt = 8;
+    if (const char* e = std::getenv("KNNSJ_TILE_QPT")) qpt = std::atoi(e);
+#define KNNSJ_TILE_LAUNCH(QPT)                                                                 \
+  do {                                                                                        \
+    if (a.K <= 16)                                                                            \
+      d3 ? launch_tile_kernel<3, 16, QPT>(p, sm_count, s) : launch_tile_kernel<2, 16, QPT>(p, sm_count, s); \
+    else if (a.K <= 33)                                                                       \
+      d3 ? launch_tile_kernel<3, 33, QPT>(p, sm_count, s) : launch_tile_kernel<2, 33, QPT>(p, sm_count, s); \
+    else                                                                                      \
+      d3 ? launch_tile_kernel<3, 65, QPT>(p, sm_count, s) : launch_tile_kernel<2, 65, QPT>(p, sm_count, s); \
+  } while (0)
+    if (qpt == 32)
+      KNNSJ_TILE_LAUNCH(32);
+    else if (qpt == 16)
+      KNNSJ_TILE_LAUNCH(16);
+    else
+      KNNSJ_TILE_LAUNCH(8);
+#undef KNNSJ_TILE_LAUNCH
+  }
+}
+
+template void launch_tile_search<float>(const SearchLaunch<float>&, uint32_t*, uint32_t*, int, cudaStream_t);
+template void launch_tile_search<double>(const SearchLaunch<double>&, uint32_t*, uint32_t*, int, cudaStream_t);
+
+}  // namespace knnsj

@@ -82,6 +82,23 @@ __device__ __forceinline__ uint32_t clamped_cell(T v, T minv, T width, uint32_t 
   return c < ncell ? c : ncell - 1;
 }
 
+// A lower (up = false) or upper (up = true) bound of the grid cell of
+// coordinate v, clamped to [0, ncell-1], from float arithmetic with a
+// reciprocal: (v - minf) * invw is within 2^-22 relative of (v - min) / width
+// (the rounding of v - minf, of 1/width, of the product, and of min and
+// width to float), plus 2^-24 |minf| * invw from rounding min; the bound
+// moves by twice that, so the true cell of any coordinate on the far side
+// of v (the grid's own monotone division in the data type) is never cut off.
+__device__ __forceinline__ uint32_t ring_cell(float v, float minf, float invw, uint32_t ncell, bool up) {
+  const float u = (v - minf) * invw;
+  const float tol = (fabsf(u) + fabsf(minf) * invw) * (1.0f / 2097152.0f) + (1.0f / 1048576.0f);
+  const float ub = up ? u + tol : u - tol;
+  if (!(ub > 0.0f)) return 0;
+  if (!(ub < (float)ncell)) return ncell - 1;
+  const uint32_t c = (uint32_t)ub;
+  return c < ncell ? c : ncell - 1;
+}
+
 // Largest squared distance accepted at radius r: the reference keeps a point
 // when acc <= fl(r*r) (SHORTCIRCUIT, kernel.cu:131-135) and sqrt(acc) <= r
 // (kernel.cu:146).  Both are monotone in acc, so one threshold decides both.
@@ -164,6 +181,16 @@ struct Key<double> {
   static __device__ __forceinline__ double acc(const type& x) { return __longlong_as_double((long long)x.a); }
   static __device__ __forceinline__ uint32_t id(const type& x) { return x.id; }
 };
+
+// The verification sum of one result row (the reference adds dist * dist,
+// GPU.cu:3690-3693): each lane's partial sum in the data type, reduced across
+// the warp in a fixed butterfly order; lane 0 stores it widened to double.
+template <typename T>
+__device__ __forceinline__ void store_row_sum(double* __restrict__ rowsum, uint64_t row, T part, int lane) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) part = Num<T>::add(part, __shfl_xor_sync(0xffffffffu, part, off));
+  if (lane == 0) rowsum[row] = (double)part;
+}
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;

@@ -100,6 +100,8 @@ void launch_eps_hist(const T* soa, uint64_t n, uint32_t d, const EpsScratch& sc,
 // GPU.cu:3690-3693) in a fixed order; result in *d_out.
 template <typename T>
 void launch_checksum(const T* dists, uint64_t count, double* d_partial, double* d_out, cudaStream_t s);
+// Sum of count doubles (the per-row verification sums) in a fixed order.
+void launch_sum_f64(const double* v, uint64_t count, double* d_partial, double* d_out, cudaStream_t s);
 
 struct GridScratch {
   unsigned long long* keys[2] = {nullptr, nullptr};
@@ -127,6 +129,17 @@ void launch_compact_cells(const unsigned long long* skeys, uint64_t n, uint32_t*
 void launch_dense_table(const unsigned long long* ckeys, const uint32_t* coff,
                         unsigned long long C, unsigned long long total_cells, uint32_t* dstart,
                         cudaStream_t s);
+// Morton (Z-order) codes of the cells of points given in cell-ordered
+// columns ps (keys) and their positions (vals), `bits` bits per dimension.
+template <typename T>
+void launch_morton_keys(const T* ps, uint64_t n, const GridGeom<T>& g, int bits, unsigned long long* keys,
+                        uint32_t* vals, cudaStream_t s);
+// Grid by counting sort (points in any order within a cell): tbl (total+1
+// entries) becomes the dense start table, ps/pid the cell-ordered columns and
+// ids of the input-order columns xs.  scan_tmp: scan_tmp_elems(total).
+template <typename T>
+void launch_counting_grid(const T* xs, uint64_t n, uint32_t d, const GridGeom<T>& g, uint32_t* tbl,
+                          uint32_t* scan_tmp, T* ps, uint32_t* pid, cudaStream_t s);
 template <typename T>
 // psf (optional): the same columns rounded to float (double data: the
 // search's float prefilter)
@@ -188,6 +201,7 @@ struct SearchLaunch {
   T step = 0;                       // radius growth written back on failure
   int32_t* out_ids = nullptr;
   T* out_d = nullptr;
+  double* rowsum = nullptr;                 // per-row verification sums, by id (nullptr: none)
   uint32_t* fail_list = nullptr;
   uint32_t* fail_count = nullptr;
   unsigned long long* cand_count = nullptr;
@@ -196,9 +210,23 @@ struct SearchLaunch {
   double coord_bound = 0.0;                 // largest |coordinate|: enables the float prefilter when finite
   SearchShape shape;                        // launch shape (autotuned for batched joins)
   const LoopCtl* ctl = nullptr;             // non-null: nq, lists and radius come from here (graph passes)
+  const uint32_t* nq_dev = nullptr;         // non-null: the pass's query count is read here (nq is a bound)
+  // tile search only: queries from these cell-ordered columns and ids (when
+  // the candidates come from another grid), visited in qorder
+  const T* qps = nullptr;
+  const uint32_t* qpid = nullptr;
+  const uint32_t* qorder = nullptr;
 };
 template <typename T>
 void launch_search(const SearchLaunch<T>& a, int sm_count, cudaStream_t s);
+// Tile search (k_tile.cu): the first pass of float data with two or three
+// dimensions, all indexed, K <= 65 and a dense cell table.  Queries it hands
+// over (ring far wider than its tile's, exact ties at the K-th distance) are
+// appended to defer_list / *defer_count for search_kernel at the same radius.
+bool tile_search_applies(uint32_t d, uint32_t di, uint32_t K, int dense, size_t elem);
+template <typename T>
+void launch_tile_search(const SearchLaunch<T>& a, uint32_t* defer_list, uint32_t* defer_count, int sm_count,
+                        cudaStream_t s);
 // Clears bytes (a multiple of 4) with a kernel: unlike a runtime memset it
 // never waits behind copies in flight on another stream.
 void launch_zero_words(void* p, size_t bytes, cudaStream_t s);
@@ -235,6 +263,10 @@ struct Workspace {
   DevBuf ckeys, coff, dstart;            // cell tables
   DevBuf list0, list1, small, eps_partial, eps_sample, perm, minmax_part, qradius;
   DevBuf chunk_list, patch_rows;         // streamed rows: queries by id block, rows finished late
+  DevBuf defer_list;                     // queries the tile search hands to search_kernel
+  DevBuf rowsum;                         // per-row verification sums (host-pointer calls)
+  DevBuf fps, fpid, fdstart;             // tile search: the finer candidate grid (columns, ids, start table)
+  DevBuf qorder;                         // tile search: cell-ordered positions in Morton order of their cells
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[8] = {};
   cudaStream_t copy_stream = nullptr;    // streamed rows: device-to-host copies
@@ -261,10 +293,13 @@ Workspace& workspace(int device);
 struct JoinConfig;
 // Full join of n x d row-major data already on the device.  h_aos (optional)
 // is the same data on the host, used for the dimension-order sample.
+// rowsum (optional, n doubles): each result row's verification sum, and
+// st->total_distance their sum.  d_ids / d_dists may be device-mapped host
+// memory: the kernels then write the rows straight into the host buffers.
 template <typename T>
 void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_aos, uint64_t n, uint32_t d,
               uint32_t k, int32_t* d_ids, T* d_dists, knnsj_stats* st, cudaStream_t s,
-              RowStream* rows = nullptr);
+              RowStream* rows = nullptr, double* rowsum = nullptr);
 template <typename T>
 void finish_row_stream(Workspace& w, const RowStream& rows, const int32_t* d_ids, const T* d_dists, uint32_t K,
                        cudaStream_t s);

@@ -75,7 +75,13 @@ typedef struct {
   int32_t verbose;          /* 1 prints phase timings on stderr [KNNSJ_VERBOSE] */
   double radius_offset;     /* KNNSJ_RADIUS_LEARNED: added to the predicted
                                log(radius / eps0); 0 = the model as trained */
-  int32_t reserved[8];
+  int32_t device_table_mb;  /* host-pointer calls with pageable outputs: the
+                               largest device result table (MB) before the
+                               outputs are registered with the device and the
+                               rows written into them directly, so that device
+                               memory holds no result table; 0 = free device
+                               memory less 2 GB [KNNSJ_DEVICE_TABLE_MB] */
+  int32_t reserved[7];
 } knnsj_options;
 
 /* Statistics of one join (all optional to read). */
@@ -106,7 +112,9 @@ typedef struct {
                                 timed out and the affected queries started at eps0 (rows stay
                                 exact); 2 as 1, and a timed-out MMA was still unconfirmed when
                                 its tensor memory was released */
-  double reserved[7];
+  double tile_handovers;     /* queries the first pass's tile search handed to the per-query
+                                search (ring far wider than its tile's, or exact ties) */
+  double reserved[6];
 } knnsj_stats;
 
 /* One independent dataset of a batched call. */
@@ -149,12 +157,16 @@ void KNNJoinPy(float* dataset, unsigned int NUMPOINTS, unsigned int kNN, unsigne
 
 /* Status-returning self-join on HOST buffers (same pipeline as KNNJoinPy,
  * dtype chosen per call).  data: row-major n x d; outputs as above.  When
- * both outputs are pinned (cudaHostAlloc / cudaHostRegister) and n >= 2^18,
- * rows are copied into them while the join runs (KNNSJ_ROW_CHUNKS blocks of
- * query ids, default 32; rows finished by later passes are written at the
- * end); pageable outputs get one copy through staging after the join.  The
- * call returns when every row is in place, also on error (no copy is left
- * in flight).  stats may be NULL. */
+ * both outputs are pinned and mapped (cudaHostAlloc, cudaHostRegister with
+ * cudaHostRegisterMapped, or any pinned buffer on a unified-addressing
+ * system), the search kernels write every row straight into them while the
+ * join runs: no device result table is allocated and nothing is copied after
+ * the join.  Pageable outputs get a device result table copied out after
+ * the join; when that table would not fit in device memory (or exceeds
+ * opts->device_table_mb), the outputs are registered with the device for the
+ * call and written directly instead.  The call returns when every row is in
+ * place, also on error (no kernel or copy is left writing into the outputs).
+ * stats may be NULL. */
 knnsj_status knnsj_selfjoin(const void* data, knnsj_dtype dtype, uint64_t n, uint32_t d,
                             uint32_t k, const knnsj_options* opts, int32_t* out_ids,
                             void* out_dists, knnsj_stats* stats);
@@ -260,6 +272,15 @@ knnsj_status knnsj_grid_dims(const void* data, knnsj_dtype dtype, uint64_t n, ui
  * only *n_points is written; then call again with out sized n_points * d. */
 knnsj_status knnsj_read_csv(const char* path, knnsj_dtype dtype, uint32_t d, void* out,
                             uint64_t* n_points);
+
+/* Binary input (no reference counterpart: the reference reads CSV only,
+ * import_dataset.cpp:50-106): a NumPy .npy file (format 1.0-3.0, C order,
+ * little-endian float32 or float64, any shape; values converted to dtype) or,
+ * without the .npy magic, raw little-endian values of dtype.  Every d
+ * consecutive values form a point; a trailing partial point is dropped.
+ * Same two-call protocol as knnsj_read_csv. */
+knnsj_status knnsj_read_binary(const char* path, knnsj_dtype dtype, uint32_t d, void* out,
+                               uint64_t* n_points);
 
 /* KNN_out.txt and KNN_out_distances.txt in directory dir, in the format of
  * printNeighborTable (main.cu:911-949).  K = k+1 entries per row. */

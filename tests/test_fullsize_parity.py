@@ -1,0 +1,118 @@
+"""Bit-exact parity with the oracle at the configurations' stated sizes.
+
+* the 25M-point 2-D sky-like join (k=64, BETA=0.025) in both radius modes,
+  every row against the oracle's full table (computed once per session);
+* the held-out 4-D 5M-point mixture at k=128 (learned and plain);
+* 1M points of the 6-D float64 mixture at k=16, BETA=0.05 (the first 1M rows
+  of the 10M-point configuration);
+* NUMINDEXEDDIM=1 (params.h:9) on a 2-D and a 4-D set;
+* the full 512-set batched configuration through knnsj_selfjoin_batched,
+  every set against the oracle's join of that set.
+
+The oracle runs on all host cores; the largest join takes a few minutes.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import hybrid_k_nearest_neighbor_self_join_gb300 as kj
+from hybrid_k_nearest_neighbor_self_join_gb300 import datasets
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__
+    __graft_entry__.build_library()
+    __graft_entry__.build_oracle()
+
+
+def device_join(x, k, di, beta, mode):
+    n, d = x.shape
+    tx = torch.from_numpy(x).cuda()
+    tids = torch.empty((n, k + 1), dtype=torch.int32, device="cuda")
+    td = torch.empty((n, k + 1), dtype=tx.dtype, device="cuda")
+    st = kj.selfjoin_device(tx.data_ptr(), x.dtype, n, d, k, tids.data_ptr(), td.data_ptr(),
+                            num_indexed_dims=di, beta=beta, radius_mode=mode)
+    torch.cuda.synchronize()
+    out = tids.cpu().numpy(), td.cpu().numpy()
+    del tx, tids, td
+    torch.cuda.empty_cache()
+    return out, st
+
+
+def assert_rows_equal(got, want):
+    (ids, dists), (oids, odists) = got, want
+    bad = np.nonzero((ids != oids).any(axis=1))[0]
+    assert bad.size == 0, f"{bad.size} rows differ in ids, first {bad[:5]}"
+    ub = np.uint32 if dists.dtype == np.float32 else np.uint64
+    bad = np.nonzero((dists.view(ub) != odists.view(ub)).any(axis=1))[0]
+    assert bad.size == 0, f"{bad.size} rows differ in distance bits, first {bad[:5]}"
+
+
+@pytest.fixture(scope="module")
+def sky_full():
+    gen, k, beta, di = datasets.CONFIGS["sky2d_25m"]
+    x = gen()
+    rc, oids, odists, _ = oracle.join(x, k, di=di, beta=beta)
+    assert rc == 0
+    return x, k, beta, di, (oids, odists)
+
+
+@pytest.mark.parametrize("mode", [kj.RADIUS_LEARNED, kj.RADIUS_PLAIN])
+def test_sky2d_25m_every_row(sky_full, mode):
+    x, k, beta, di, want = sky_full
+    got, st = device_join(x, k, di, beta, mode)
+    assert_rows_equal(got, want)
+
+
+@pytest.fixture(scope="module")
+def heldout_full():
+    gen, k, beta, di = datasets.CONFIGS["heldout4d_5m"]
+    x = gen()
+    rc, oids, odists, _ = oracle.join(x, k, di=di, beta=beta)
+    assert rc == 0
+    return x, k, beta, di, (oids, odists)
+
+
+@pytest.mark.parametrize("mode", [kj.RADIUS_LEARNED, kj.RADIUS_PLAIN])
+def test_heldout4d_5m_k128_every_row(heldout_full, mode):
+    x, k, beta, di, want = heldout_full
+    got, st = device_join(x, k, di, beta, mode)
+    assert_rows_equal(got, want)
+
+
+def test_gmm6d_double_1m_every_row():
+    x = np.ascontiguousarray(datasets.gmm6d(10_000_000, 2)[:1_000_000])
+    k, beta, di = 16, 0.05, 6
+    rc, oids, odists, _ = oracle.join(x, k, di=di, beta=beta)
+    assert rc == 0
+    for mode in (kj.RADIUS_PLAIN, kj.RADIUS_LEARNED):
+        got, st = device_join(x, k, di, beta, mode)
+        assert_rows_equal(got, (oids, odists))
+
+
+@pytest.mark.parametrize("d", [2, 4])
+def test_one_indexed_dimension(d):
+    x = datasets.gmm(200_000, d, 12, 0.2, 30 + d, dtype=np.float32)
+    k, beta = 16, 0.05
+    rc, oids, odists, _ = oracle.join(x, k, di=1, beta=beta)
+    assert rc == 0
+    for mode in (kj.RADIUS_PLAIN, kj.RADIUS_LEARNED):
+        got, st = device_join(x, k, 1, beta, mode)
+        assert_rows_equal(got, (oids, odists))
+
+
+def test_batched_512_sets_against_oracle():
+    sets = list(datasets.batched_sets())
+    assert len(sets) == 512
+    outs = kj.selfjoin_batched([x for x, _ in sets], [k for _, k in sets], beta=0.05,
+                               radius_mode=kj.RADIUS_LEARNED)
+    for i, ((x, k), (ids, dists)) in enumerate(zip(sets, outs)):
+        rc, oids, odists, _ = oracle.join(x, k, di=min(x.shape[1], 6), beta=0.05)
+        assert rc == 0, i
+        assert np.array_equal(ids, oids), f"set {i}: ids differ"
+        assert np.array_equal(dists.view(np.uint32), odists.view(np.uint32)), f"set {i}: distances differ"

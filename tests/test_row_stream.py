@@ -1,9 +1,16 @@
-"""Host-pointer joins into pinned output buffers stream their rows out while
-the join runs: blocks of query ids searched one after another in the first
-pass, each block's rows copied out on a second stream, and the rows finished
-by later passes written into the host buffers at the end.  The rows must equal
-those of a join into ordinary (pageable) buffers, which come back in one copy
-after the join."""
+"""Where the rows of host-pointer joins go, and that they are the same rows.
+
+* pinned, mapped output buffers: the search kernels write every row straight
+  into them (no device result table, no copy after the join);
+* pageable buffers whose result table is larger than the device-table cap
+  (opts->device_table_mb, the memory-bounded mode): the buffers are registered
+  with the device for the call and written the same way;
+* with direct rows off (KNNSJ_DIRECT_ROWS=0), pinned buffers take their rows
+  in blocks of query ids copied out while the join runs, later passes' rows
+  patched in at the end.
+Each must equal a join into ordinary pageable buffers (a device table copied
+out in one piece after the join), including the verification sum.
+"""
 import numpy as np
 import pytest
 
@@ -27,20 +34,29 @@ def pinned(shape, np_dtype):
     return t, t.numpy()
 
 
-@pytest.mark.parametrize("mode,chunks,dtype,graph", [(kj.RADIUS_LEARNED, "8", np.float32, "1"),
-                                                     (kj.RADIUS_PLAIN, "3", np.float32, "1"),
-                                                     (kj.RADIUS_LEARNED, "32", np.float64, "1"),
-                                                     (kj.RADIUS_PLAIN, "8", np.float32, "0")])
-def test_streamed_rows_match_one_copy(monkeypatch, mode, chunks, dtype, graph):
-    # graph "0": the passes after the first are driven from the host
+def reference(x, k, mode, monkeypatch):
+    # pageable outputs, device table copied out after the join
+    ref_i, ref_d, st = kj.selfjoin(x, k, beta=0.025, radius_mode=mode, return_stats=True)
+    # another join of the same size leaves other rows in the device tables,
+    # so a row a later join failed to deliver cannot match by chance
+    y = datasets.uniform(x.shape[0], x.shape[1], 32).astype(x.dtype)
+    kj.selfjoin(y, k, beta=0.025, radius_mode=mode)
+    return ref_i, ref_d, st["total_distance"]
+
+
+def same(ids, dd, ref_i, ref_d):
+    assert np.array_equal(ids, ref_i)
+    bits = np.uint32 if dd.dtype == np.float32 else np.uint64
+    assert np.array_equal(dd.view(bits), ref_d.view(bits))
+
+
+@pytest.mark.parametrize("mode,dtype,graph", [(kj.RADIUS_LEARNED, np.float32, "1"),
+                                              (kj.RADIUS_PLAIN, np.float32, "0"),
+                                              (kj.RADIUS_LEARNED, np.float64, "1")])
+def test_direct_rows_into_pinned_buffers(monkeypatch, mode, dtype, graph):
     n, k = 400_000, 32
     x = datasets.sky_like(n, seed=31).astype(dtype)
-    ref_i, ref_d = kj.selfjoin(x, k, beta=0.025, radius_mode=mode)
-    # another join of the same size leaves other rows in the device tables,
-    # so a row the streamed join failed to deliver cannot match by chance
-    y = datasets.uniform(n, 2, 32).astype(dtype)
-    kj.selfjoin(y, k, beta=0.025, radius_mode=mode)
-    monkeypatch.setenv("KNNSJ_ROW_CHUNKS", chunks)
+    ref_i, ref_d, ref_sum = reference(x, k, mode, monkeypatch)
     monkeypatch.setenv("KNNSJ_GRAPH", graph)
     t_i, ids = pinned((n, k + 1), np.int32)
     t_d, dd = pinned((n, k + 1), dtype)
@@ -48,17 +64,39 @@ def test_streamed_rows_match_one_copy(monkeypatch, mode, chunks, dtype, graph):
     dd[:] = np.nan
     _, _, st = kj.selfjoin(x, k, beta=0.025, radius_mode=mode, out_ids=ids, out_dists=dd, return_stats=True)
     assert st["queries_run"] > n  # some rows were finished after the first pass
-    assert np.array_equal(ids, ref_i)
-    bits = np.uint32 if dtype == np.float32 else np.uint64
-    assert np.array_equal(dd.view(bits), ref_d.view(bits))
+    same(ids, dd, ref_i, ref_d)
+    assert st["total_distance"] == ref_sum
 
 
-def test_small_outputs_come_back_in_one_copy():
-    # below the streaming size a pinned buffer takes the single copy
-    n, k = 50_000, 8
-    x = datasets.uniform(n, 3, 33)
-    ref_i, ref_d = kj.selfjoin(x, k)
+@pytest.mark.parametrize("mode", [kj.RADIUS_LEARNED, kj.RADIUS_PLAIN])
+def test_memory_bounded_pageable_outputs(monkeypatch, mode):
+    # a 1 MB cap on the device result table: the pageable outputs are
+    # registered for the call and receive their rows directly
+    n, k = 300_000, 64
+    x = datasets.sky_like(n, seed=41)
+    ref_i, ref_d, ref_sum = reference(x, k, mode, monkeypatch)
+    ids = np.full((n, k + 1), -7, np.int32)
+    dd = np.full((n, k + 1), np.nan, np.float32)
+    _, _, st = kj.selfjoin(x, k, beta=0.025, radius_mode=mode, out_ids=ids, out_dists=dd, return_stats=True,
+                           device_table_mb=1)
+    same(ids, dd, ref_i, ref_d)
+    assert st["total_distance"] == ref_sum
+
+
+@pytest.mark.parametrize("mode,chunks,graph", [(kj.RADIUS_LEARNED, "8", "1"), (kj.RADIUS_PLAIN, "3", "0")])
+def test_streamed_rows_match_one_copy(monkeypatch, mode, chunks, graph):
+    n, k = 400_000, 32
+    x = datasets.sky_like(n, seed=31)
+    ref_i, ref_d, ref_sum = reference(x, k, mode, monkeypatch)
+    monkeypatch.setenv("KNNSJ_DIRECT_ROWS", "0")
+    monkeypatch.setenv("KNNSJ_ROW_CHUNKS", chunks)
+    monkeypatch.setenv("KNNSJ_GRAPH", graph)
     t_i, ids = pinned((n, k + 1), np.int32)
     t_d, dd = pinned((n, k + 1), np.float32)
-    kj.selfjoin(x, k, out_ids=ids, out_dists=dd)
-    assert np.array_equal(ids, ref_i) and np.array_equal(dd, ref_d)
+    ids[:] = -7
+    dd[:] = np.nan
+    _, _, st = kj.selfjoin(x, k, beta=0.025, radius_mode=mode, out_ids=ids, out_dists=dd, return_stats=True)
+    same(ids, dd, ref_i, ref_d)
+    # (rows may be written by the other search kernel here, whose per-row sum
+    # adds the same values in another order)
+    assert abs(st["total_distance"] - ref_sum) <= 1e-6 * abs(ref_sum)
