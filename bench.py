@@ -186,6 +186,75 @@ def workload_config(n: int, d: int, k: int, beta: float, di: int) -> dict:
             "l2": "inputs (200 MB) and outputs (13 GB) exceed the 129 MB L2; no flush"}
 
 
+def config_records(kj, torch, steps: int = 2) -> dict:
+    """The other configurations, device-resident, learned and plain starting
+    radius on the same data with their tables compared bit for bit: the
+    uniform 100k-point 2-D set (k=8, BETA=0), the 10M-point 6-D float64
+    mixture (k=16, BETA=0.05), the held-out 5M-point 4-D mixture (k=128), and
+    the 512 uneven sets through the batched host API (learned radius)."""
+    import numpy as np
+
+    from hybrid_k_nearest_neighbor_self_join_gb300 import datasets
+    out = {}
+    fp64_peak = 1.25e12  # nominal GB300 FP64 FLOP/s
+    for name in ("uniform2d_100k", "gmm6d_10m", "heldout4d_5m"):
+        gen, k, beta, di = datasets.CONFIGS[name]
+        x = gen()
+        n, d = x.shape
+        tx = torch.from_numpy(x).cuda()
+        tids = torch.empty((n, k + 1), dtype=torch.int32, device="cuda")
+        td = torch.empty((n, k + 1), dtype=tx.dtype, device="cuda")
+        rec = {"n_points": n, "d": d, "k": k, "beta": beta, "num_indexed_dims": di, "dtype": str(x.dtype)}
+        tables = {}
+        for label, mode in (("learned", kj.RADIUS_LEARNED), ("plain", kj.RADIUS_PLAIN)):
+            kj.selfjoin_device(tx.data_ptr(), x.dtype, n, d, k, tids.data_ptr(), td.data_ptr(),
+                               num_indexed_dims=di, beta=beta, radius_mode=mode)  # warm-up
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            sts = [kj.selfjoin_device(tx.data_ptr(), x.dtype, n, d, k, tids.data_ptr(), td.data_ptr(),
+                                      num_indexed_dims=di, beta=beta, radius_mode=mode) for _ in range(steps)]
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            st = sts[-1]
+            r = {"ms_per_join": ms, "queries_per_s": n / (ms / 1e3), "iterations": st["iterations"],
+                 "queries_run": st["queries_run"], "re_attempts": st["queries_run"] - n,
+                 "candidates": st["candidates"], "ms_search_kernels": st["ms_search_kernels"],
+                 "regrids": st["regrids"]}
+            if x.dtype == np.float64:
+                # FP64 arithmetic of the candidates a double join evaluates
+                # (3d per candidate), against the nominal FP64 rate; the float
+                # prefilter moves most of it to the FP32 pipe
+                r["fp64_frac_of_nominal"] = st["search_alg_flops"] / (st["ms_search_kernels"] / 1e3) / fp64_peak
+                r["hbm_gbs_alg"] = st["search_alg_bytes"] / (st["ms_search_kernels"] / 1e3) / 1e9
+            rec[label] = r
+            tables[label] = (tids.clone(), td.clone())
+        a, b = tables["learned"], tables["plain"]
+        bits = torch.int32 if x.dtype == np.float32 else torch.int64
+        rec["identical_to_plain"] = bool(torch.equal(a[0], b[0]) and torch.equal(a[1].view(bits), b[1].view(bits)))
+        rec["learned_over_plain"] = rec["plain"]["ms_per_join"] / rec["learned"]["ms_per_join"]
+        out[name] = rec
+        del tx, tids, td, tables, a, b
+        torch.cuda.empty_cache()
+    # 512 uneven sets, batched host API (host buffers: copies included)
+    sets = list(datasets.batched_sets())
+    xs = [x for x, _ in sets]
+    ks = [k for _, k in sets]
+    kj.selfjoin_batched(xs, ks, beta=0.05, radius_mode=kj.RADIUS_LEARNED)  # warm-up (and autotuning)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        kj.selfjoin_batched(xs, ks, beta=0.05, radius_mode=kj.RADIUS_LEARNED)
+        times.append(time.perf_counter() - t0)
+    npts = sum(x.shape[0] for x in xs)
+    out["batched_512"] = {"sets": len(sets), "n_points": npts, "ms_per_call": 1e3 * statistics.median(times),
+                          "queries_per_s": npts / statistics.median(times),
+                          "note": "host buffers in and out (copies inside the timing), learned radius"}
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -297,9 +366,9 @@ def run_gb300(args):
     t_e2e = dist.max(marks[0].elapsed_time(marks[-1]))
     e2e_value = n * world * e2e_steps / (t_e2e / 1e3)
     e2e_ms_steps = [round(marks[i].elapsed_time(marks[i + 1]), 2) for i in range(e2e_steps)]
-    # rows were streamed to the host during the join when the copies that
-    # outlast it are short (one copy of the 13 GB table after the join takes
-    # tens of ms)
+    # rows reached the host during the join (written straight into the
+    # pinned buffers) when no copy outlasted it: one copy of the 13 GB table
+    # after the join takes tens of ms
     e2e_streamed = all(s_["ms_transfer"] < 0.5 * s_["ms_search"] for s_ in e2e_stats)
 
     # ---- roofline of the dominant kernel (the search) ----------------------
@@ -315,7 +384,8 @@ def run_gb300(args):
     fp32_ach = fl / (kms / 1e3) / 1e12
     roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"], "traffic": tr["dram_bytes_per_join"] if tr else None,
-                "kernel": "search_kernel<float,2,2>", "kernel_ms_per_step": kms, "launches_per_step":
+                "kernel": ("search kernels: tile_kernel<2,65,8> (first pass, query tiles) + search_kernel<float,2,2> "
+                           "(retries and hand-overs)"), "kernel_ms_per_step": kms, "launches_per_step":
                 st["iterations"], "alg_bytes_per_step": ab,
                 "peak_source": f"{pk['source']} hbm_gbs (MEASURED_PEAKS.json): frac is of {pk['source']}",
                 "fp32": {"achieved_tflops": fp32_ach, "peak_tflops": fp32_peak, "frac": fp32_ach / fp32_peak,
@@ -333,7 +403,7 @@ def run_gb300(args):
                 "steps_detail": [{"ms_prep": round(s_["ms_prep"], 2), "ms_search": round(s_["ms_search"], 2),
                                   "ms_transfer": round(s_["ms_transfer"], 2), "iterations": s_["iterations"]}
                                  for s_ in e2e_stats],
-                "rows_streamed_during_join": e2e_streamed},
+                "rows_written_during_join": e2e_streamed},
         "gpu_launches": launches,
         "roofline": roofline,
         "clocks": clk,
@@ -345,6 +415,10 @@ def run_gb300(args):
         "stats_last_step": {kk: st[kk] for kk in ("eps0", "iterations", "regrids", "candidates", "queries_run",
                                                   "ms_prep", "ms_search", "ms_search_kernels", "nonempty_cells")},
     }
+    if rank == 0 and world == 1 and not args.no_configs:
+        del tx, tids, td
+        torch.cuda.empty_cache()
+        line["configs"] = config_records(kj, torch)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, k, beta, di, args.cpu_sample)
     if rank == 0:
@@ -388,6 +462,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=250_000,
                     help="queries the CPU baseline searches per step (1%% of the 25M-point workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other configurations' records")
     ap.add_argument("--profile-case", choices=["full", "slice"], default=None,
                     help="run one join for a profiler capture and exit")
     ap.add_argument("--profile-mode", choices=["learned", "plain"], default="learned")

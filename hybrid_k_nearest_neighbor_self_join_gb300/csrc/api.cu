@@ -54,7 +54,7 @@ knnsj_status make_config(const knnsj_options* o, uint32_t d, JoinConfig* c) {
   if (const char* e = env("KNNSJ_ROW_CHUNKS")) c->row_chunks = std::atoi(e);
   if (const char* e = env("KNNSJ_TAIL_BRUTE")) c->tail_brute = std::atoi(e);
   if (const char* e = env("KNNSJ_TILE")) c->tile_search = std::atoi(e);
-  if (const char* e = env("KNNSJ_TILE_FINE")) c->tile_fine = std::max(1, std::atoi(e));
+  if (const char* e = env("KNNSJ_TILE_FINE")) c->tile_fine = std::max(0, std::atoi(e));
   if (const char* e = env("KNNSJ_DIRECT_ROWS")) c->direct_rows = std::atoi(e);
   if (const char* e = env("KNNSJ_DEVICE_TABLE_MB")) c->device_table_cap = (unsigned long long)std::atoll(e) << 20;
   if (const char* e = env("KNNSJ_SEARCH_SHAPE")) {  // "warps,qchunk,buffer" (0 = default)

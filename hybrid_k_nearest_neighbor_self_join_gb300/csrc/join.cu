@@ -458,33 +458,36 @@ struct TileSetup {
 };
 
 template <typename T>
-static void prepare_tile(Workspace& w, const JoinConfig& cfg, const DeviceGrid<T>& g, const T* xs, uint64_t n,
+static void prepare_tile(Workspace& w, bool tiles, int fine_max, const DeviceGrid<T>& g, const T* xs, uint64_t n,
                          uint32_t d, T eps0, const std::vector<T>& mx, TileSetup<T>* t, cudaStream_t s) {
   const uint32_t di = g.geom.di;
+  GridScratch sc;
+  sc.hist_elems = radix_hist_elems(n);
+  sc.scan_tmp_elems = scan_tmp_elems(std::max<size_t>(sc.hist_elems, n + 1));
+  t->per_query = !tiles;
+  if (tiles) {
   // 1. Morton order of the eps0 cells (stable: cell order within a cell)
   int bits = 1;
   for (uint32_t j = 0; j < di; j++)
     while (bits < 21 && (1ull << bits) < (unsigned long long)g.geom.ncell[j]) bits++;
-  GridScratch sc;
   sc.keys[0] = (unsigned long long*)w.keys0.get(n * 8);
   sc.keys[1] = (unsigned long long*)w.keys1.get(n * 8);
   sc.vals[0] = (uint32_t*)w.vals0.get(n * 4);
   sc.vals[1] = (uint32_t*)w.vals1.get(n * 4);
-  sc.hist_elems = radix_hist_elems(n);
   sc.hist = (uint32_t*)w.hist.get(sc.hist_elems * 4);
-  sc.scan_tmp_elems = scan_tmp_elems(std::max<size_t>(sc.hist_elems, n + 1));
   sc.scan_tmp = (uint32_t*)w.scan_tmp.get(sc.scan_tmp_elems * 4);
   launch_morton_keys<T>(g.ps, n, g.geom, bits, sc.keys[0], sc.vals[0], s);
   const int cur = radix_sort_pairs(sc, n, bits * (int)di, s);
   uint32_t* qorder = (uint32_t*)w.qorder.get(n * 4);
   dev_copy(w, qorder, sc.vals[cur], n * 4, s);
   t->qorder = qorder;
-  // 2. candidate grid: width eps0 / f, the largest f <= cfg.tile_fine whose
+  }
+  // 2. candidate grid: width eps0 / f, the largest f <= fine_max whose
   // dense table stays within max(8 n, 2^24) cells
   t->cand = g;
   t->fine = 1;
   const unsigned long long limit = std::max<unsigned long long>(8ull * n, 1ull << 24);
-  for (int f = cfg.tile_fine; f >= 2; f--) {
+  for (int f = fine_max; f >= 2; f--) {
     GridGeom<T> gf = g.geom;
     gf.width = (T)((double)eps0 / (double)f);
     if (!(gf.width > 0)) continue;
@@ -522,7 +525,6 @@ static void prepare_tile(Workspace& w, const JoinConfig& cfg, const DeviceGrid<T
     break;
   }
   t->on = true;
-  t->per_query = cfg.tile_search == 2;
 }
 
 // One search pass over the queries of a.qlist (or all points in cell order):
@@ -831,8 +833,14 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   // 5b. the first pass's tile search (2-D / 3-D float data, all indexed)
   TileSetup<T> tile;
   const bool will_stream = rows && rows->chunks >= 2 && n >= (uint64_t)rows->chunks;
-  if (cfg.tile_search && !will_stream && tile_search_applies(d, di, K, P.grid.dense, sizeof(T)))
-    prepare_tile<T>(w, cfg, P.grid, P.xs, n, d, P.eps0, P.mx, &tile, s);
+  if (cfg.tile_search && !will_stream && tile_search_applies(d, di, K, P.grid.dense, sizeof(T))) {
+    // per-query starting radii: query tiles over a grid of width eps0/4; a
+    // uniform radius: one warp per query over a grid of width eps0/2
+    // (measured best for each on the 25M-point sky-like set)
+    const bool tiles = cfg.tile_search == 3 || (cfg.tile_search == 1 && qrad != nullptr);
+    const int fine = cfg.tile_fine > 0 ? cfg.tile_fine : (tiles ? 4 : 2);
+    prepare_tile<T>(w, tiles, fine, P.grid, P.xs, n, d, P.eps0, P.mx, &tile, s);
+  }
 
   // 6. retry loop (main.cu:312-430)
   uint32_t* list[2] = {(uint32_t*)w.list0.get(n * 4), (uint32_t*)w.list1.get(n * 4)};

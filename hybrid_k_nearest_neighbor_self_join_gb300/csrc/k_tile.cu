@@ -16,7 +16,7 @@
 //      to search_kernel instead, so one outlier does not widen everyone's
 //      scan); each ring row of the box (consecutive cells along dimension 0)
 //      is one contiguous run of the cell-ordered columns;
-//   2. candidates are staged in shared memory 128 at a time (coalesced
+//   2. candidates are staged in shared memory 64 at a time (coalesced
 //      loads: coordinates and id in one 16-byte record) and read back by every
 //      lane at once (broadcast);
 //   3. pass 1: each lane counts its candidates within its own radius in 32
@@ -49,7 +49,7 @@ namespace {
 
 constexpr int TILE_WARPS = 4;                    // warps per block
 constexpr int TILE_THREADS = TILE_WARPS * 32;
-constexpr int TILE_CH = 128;                     // staged candidates per chunk
+constexpr int TILE_CH = 64;                      // staged candidates per chunk
 constexpr int TILE_BINS = 32;
 constexpr int TILE_OV = 16;                      // overflow keys per lane
 constexpr int TILE_OV_PITCH = TILE_OV + 1;       // u64 words per lane (odd: spreads banks)
@@ -123,13 +123,13 @@ __device__ __forceinline__ void warp_append(bool want, uint32_t v, uint32_t* lis
   if (want) list[base + __popc(m & lanemask_lt())] = v;
 }
 
-// QPT queries per warp (8, 16 or 32), LPQ = 32 / QPT lanes per query: lane
+// QPT queries per warp (4, 8 or 16), LPQ = 32 / QPT lanes per query: lane
 // (slot qs = lane % QPT, phase ph = lane / QPT) evaluates the staged
 // candidates ph, ph + LPQ, ... for query qs.  The query's lanes share its
 // histogram, row and overflow list through shared-memory atomics; the lane
 // of phase 0 does the query's serial steps.
 template <int D, int KMAX, int QPT>
-__global__ void __launch_bounds__(TILE_THREADS, 4) tile_kernel(const TileParams p) {
+__global__ void __launch_bounds__(TILE_THREADS, 5) tile_kernel(const TileParams p) {
   using SM = TileSmem<QPT, KMAX>;
   constexpr int LPQ = 32 / QPT;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -192,26 +192,14 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) tile_kernel(const TileParams 
       hi[j] = ring_cell(q[j] + rf + slack, s_minf[j], s_invw, p.g.ncell[j], true);
       ext = max(ext, hi[j] - lo[j] + 1);
     }
-    // queries whose ring is far wider than the tile's median go to search_kernel
+    // queries whose ring is far wider than the tile's mean go to search_kernel
+    // (one outlier would widen every query's scan)
     bool defer = false;
     {
-      const uint32_t e = valid ? ext : 0xffffffffu;
-      unsigned long long key = ((unsigned long long)e << 32) | (unsigned)lane;
-#pragma unroll
-      for (int kk = 2; kk <= 32; kk <<= 1) {
-#pragma unroll
-        for (int jj = kk >> 1; jj > 0; jj >>= 1) {
-          const unsigned long long o = __shfl_xor_sync(FULL, key, jj);
-          const bool up = (lane & kk) == 0;
-          const bool low = (lane & jj) == 0;
-          const unsigned long long mn = key < o ? key : o;
-          const unsigned long long mx = key < o ? o : key;
-          key = (low == up) ? mn : mx;
-        }
-      }
-      const int nvalid = __popc(__ballot_sync(FULL, valid));  // (each query counted LPQ times)
-      const uint32_t med = (uint32_t)(__shfl_sync(FULL, key, (nvalid - 1) >> 1) >> 32);
-      defer = valid && ext > 2u * med + 2u;
+      const uint32_t nv = __popc(__ballot_sync(FULL, valid));  // (each query counted LPQ times)
+      const uint32_t sum = __reduce_add_sync(FULL, valid ? ext : 0u);
+      const uint32_t mean = (sum + nv - 1) / nv;
+      defer = valid && ext > 2u * mean + 2u;
     }
     bool in = valid && !defer;  // queries searched by this tile
     uint32_t LO[D], HI[D];
@@ -330,6 +318,51 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) tile_kernel(const TileParams 
       for (int b = ph; b < TILE_BINS; b += LPQ) h[b] = 0u;
     };
 
+    // The boundary search over one query's 32 bins (counts h[b], base keys
+    // below bin 0), shared by its LPQ lanes: each lane sums its 32 / LPQ
+    // consecutive bins, a scan over the query's lanes gives each lane its
+    // starting count, and the lane holding the bin where the count reaches K
+    // reports it.  With `prefix` the bins are replaced by their exclusive
+    // prefix (plus base).  Outputs are the query's (same on its lanes).
+    auto walk_bins = [&](uint32_t* h, uint32_t base, bool prefix, uint32_t& total, uint32_t& lo_cnt,
+                         uint32_t& mb, uint32_t& bstar) {
+      constexpr int BPL = TILE_BINS / LPQ;
+      uint32_t part = 0;
+#pragma unroll
+      for (int i = 0; i < BPL; i++) part += h[ph * BPL + i];
+      uint32_t incl = part;
+#pragma unroll
+      for (int off = 1; off < LPQ; off <<= 1) {
+        const uint32_t tt = __shfl_up_sync(FULL, incl, off * QPT);
+        if (ph >= off) incl += tt;
+      }
+      uint32_t cum = base + incl - part;
+      uint32_t fb = TILE_BINS, flo = 0, fm = 0;
+#pragma unroll
+      for (int i = 0; i < BPL; i++) {
+        const int b = ph * BPL + i;
+        const uint32_t hh = h[b];
+        if (prefix) h[b] = cum;
+        if (fb == TILE_BINS && cum + hh >= K) {
+          fb = (uint32_t)b;
+          flo = cum;
+          fm = hh;
+        }
+        cum += hh;
+      }
+      total = __shfl_sync(FULL, base + incl, qs + QPT * (LPQ - 1)) - base;
+      // the first lane of the query (by phase) that found the boundary
+      const unsigned hit = __ballot_sync(FULL, fb != TILE_BINS);
+      unsigned qmask = 0;
+#pragma unroll
+      for (int pp = 0; pp < LPQ; pp++) qmask |= 1u << (qs + QPT * pp);
+      const unsigned mine = hit & qmask;
+      const int src = mine ? __ffs(mine) - 1 : qs;
+      bstar = __shfl_sync(FULL, fb, src);
+      lo_cnt = __shfl_sync(FULL, flo, src);
+      mb = __shfl_sync(FULL, fm, src);
+    };
+
     // 3. pass 1: counts per bin of squared distance within the radius
     clear_bins(hq);
     __syncwarp();
@@ -340,27 +373,11 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) tile_kernel(const TileParams 
     // candidates evaluated: the union box's points for every query it serves
     scanned += (unsigned long long)box_points * (unsigned)__popc(__ballot_sync(FULL, in && lead));
     __syncwarp();
-    // boundary bin of level 0 and the counts below it (the query's lead lane);
-    // its bins become the exclusive prefix
+    // boundary bin of level 0 and the counts below it; the query's LPQ lanes
+    // each take 32 / LPQ consecutive bins, and its bins become the exclusive
+    // prefix
     uint32_t found = 0, c_lo = 0, m = 0, bs0 = TILE_BINS;
-    if (lead) {
-      uint32_t cum = 0;
-      for (int b = 0; b < TILE_BINS; b++) {
-        const uint32_t h = hq[b];
-        hq[b] = cum;
-        if (bs0 == TILE_BINS && cum + h >= K) {
-          bs0 = (uint32_t)b;
-          c_lo = cum;
-          m = h;
-        }
-        cum += h;
-      }
-      found = cum;
-    }
-    found = __shfl_sync(FULL, found, qs);
-    c_lo = __shfl_sync(FULL, c_lo, qs);
-    m = __shfl_sync(FULL, m, qs);
-    bs0 = __shfl_sync(FULL, bs0, qs);
+    walk_bins(hq, 0u, true, found, c_lo, m, bs0);
     bool ok = in && found >= K;
     // refinement of the boundary bin while it overflows the overflow list
     int lev = 0;
@@ -387,22 +404,8 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) tile_kernel(const TileParams 
         }
       });
       __syncwarp();
-      uint32_t nb = TILE_BINS, nlo = c_lo, nm = m;
-      if (need && lead) {
-        uint32_t cum = c_lo;
-        for (int b = 0; b < TILE_BINS; b++) {
-          const uint32_t h = aq[b];
-          if (nb == TILE_BINS && cum + h >= K) {
-            nb = (uint32_t)b;
-            nlo = cum;
-            nm = h;
-          }
-          cum += h;
-        }
-      }
-      nb = __shfl_sync(FULL, nb, qs);
-      nlo = __shfl_sync(FULL, nlo, qs);
-      nm = __shfl_sync(FULL, nm, qs);
+      uint32_t nb = TILE_BINS, nlo = c_lo, nm = m, ntot = 0;
+      walk_bins(aq, c_lo, false, ntot, nlo, nm, nb);
       if (need) {
         bs[L] = (int)nb;
         c_lo = nlo;
@@ -426,73 +429,64 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) tile_kernel(const TileParams 
         const float acc = sqdist(c);
         if (live && ok && acc <= thr) {
           const int b0 = tbin(acc, sl[0], MAG);
-          int slot_bin = -1;
-          bool over = false;
-          if (b0 < bs[0]) {
-            slot_bin = b0;
-          } else if (b0 == bs[0]) {
-            if (lev == 0) {
-              over = true;
-            } else {
-              const int b1 = tbin(acc, sl[1], MAG + cl[1]);
-              if (b1 < bs[1]) {
-                slot_bin = b0;
-              } else if (b1 == bs[1]) {
-                if (lev == 1) {
-                  over = true;
-                } else {
-                  const int b2 = tbin(acc, sl[2], MAG + cl[2]);
-                  if (b2 < bs[2])
-                    slot_bin = b0;
-                  else if (b2 == bs[2])
-                    over = true;
-                }
+          bool place = b0 < bs[0];
+          bool over = b0 == bs[0] && lev == 0;
+          if (b0 == bs[0] && lev > 0) {  // (refined boundary bins only)
+            const int b1 = tbin(acc, sl[1], MAG + cl[1]);
+            if (b1 < bs[1]) {
+              place = true;
+            } else if (b1 == bs[1]) {
+              if (lev == 1) {
+                over = true;
+              } else {
+                const int b2 = tbin(acc, sl[2], MAG + cl[2]);
+                place = b2 < bs[2];
+                over = b2 == bs[2];
               }
             }
           }
           const unsigned long long key = ((unsigned long long)__float_as_uint(acc) << 32) | c.id;
-          if (slot_bin >= 0) myrow[atomicAdd(&hq[slot_bin], 1u)] = key;
+          if (place) myrow[atomicAdd(&hq[b0], 1u)] = key;
           if (over) myov[atomicAdd(ovc, 1u)] = key;
         }
       });
     }
     __syncwarp();
 
-    // 5. rows in order: insertion sort (keys are already grouped by bin);
-    // the overflow list is sorted by a second lane of the query when there
-    // is one, and its smallest keys complete the row
-    const bool sorter_row = ok && lead;
-    const bool sorter_ov = ok && (LPQ > 1 ? ph == 1 : lead);
+    // 5. rows in order: after pass 2, bin b < bs0 holds slots [hq[b-1], hq[b])
+    // and the placed part of the boundary bin [hq[bs0-1], hq[bs0]); the
+    // query's lanes insertion-sort these short ranges (keys of one bin) in
+    // parallel, one lane also sorts the overflow list, and the smallest
+    // overflow keys complete the row
     const uint32_t nov = *ovc;
-    if (sorter_row) {
-      for (uint32_t i = 1; i < c_lo; i++) {
-        const unsigned long long key = myrow[i];
+    auto isort = [](unsigned long long* a, uint32_t lo, uint32_t hi) {
+      for (uint32_t i = lo + 1; i < hi; i++) {
+        const unsigned long long key = a[i];
         uint32_t j = i;
-        while (j > 0) {
-          const unsigned long long prev = myrow[j - 1];
+        while (j > lo) {
+          const unsigned long long prev = a[j - 1];
           if (prev <= key) break;
-          myrow[j] = prev;
+          a[j] = prev;
           j--;
         }
-        myrow[j] = key;
+        a[j] = key;
       }
-    }
-    if (sorter_ov) {
-      for (uint32_t i = 1; i < nov; i++) {
-        const unsigned long long key = myov[i];
-        uint32_t j = i;
-        while (j > 0) {
-          const unsigned long long prev = myov[j - 1];
-          if (prev <= key) break;
-          myov[j] = prev;
-          j--;
-        }
-        myov[j] = key;
+    };
+    if (ok) {
+      constexpr int BPL = TILE_BINS / LPQ;
+#pragma unroll 1
+      for (int i = 0; i < BPL; i++) {
+        const int b = ph * BPL + i;
+        if (b > bs[0]) break;
+        const uint32_t lo_s = b == 0 ? 0u : hq[b - 1];
+        const uint32_t hi_s = hq[b];
+        if (hi_s - lo_s > 1) isort(myrow, lo_s, hi_s);
       }
+      if (ph == LPQ - 1) isort(myov, 0u, nov);
     }
     __syncwarp();
-    if (sorter_row)
-      for (uint32_t i = c_lo; i < K; i++) myrow[i] = myov[i - c_lo];
+    if (ok)
+      for (uint32_t i = c_lo + (uint32_t)ph; i < K; i += LPQ) myrow[i] = myov[i - c_lo];
     __syncwarp();
     // coalesced row writes: the warp writes each accepted query's row
     {
@@ -606,10 +600,10 @@ void launch_tile_search(const SearchLaunch<T>& a, uint32_t* defer_list, uint32_t
     else                                                                                      \
       d3 ? launch_tile_kernel<3, 65, QPT>(p, sm_count, s) : launch_tile_kernel<2, 65, QPT>(p, sm_count, s); \
   } while (0)
-    if (qpt == 32)
-      KNNSJ_TILE_LAUNCH(32);
-    else if (qpt == 16)
+    if (qpt == 16)
       KNNSJ_TILE_LAUNCH(16);
+    else if (qpt == 4)
+      KNNSJ_TILE_LAUNCH(4);
     else
       KNNSJ_TILE_LAUNCH(8);
 #undef KNNSJ_TILE_LAUNCH

@@ -35,8 +35,11 @@ struct JoinConfig {
                                            // an exact scan over all points (2: at any due rebuild; 0: off)
   int row_chunks = 32;                     // host-pointer calls into pinned buffers: rows streamed out
                                            // in this many blocks while the join runs (< 2: at the end)
-  int tile_search = 1;                     // first pass of 2-D / 3-D float data by query tiles (k_tile.cu)
-  int tile_fine = 4;                       // its candidate grid: eps0 / tile_fine cells (1: the eps0 grid)
+  int tile_search = 1;                     // first pass of 2-D / 3-D float data over a finer grid: 0 off,
+                                           // 1 query tiles (k_tile.cu) for per-query radii and one warp
+                                           // per query for a uniform radius, 2 always one warp per query,
+                                           // 3 always query tiles
+  int tile_fine = 0;                       // that grid's cells: eps0 / tile_fine (0: 4 for tiles, 2 else)
   int direct_rows = 1;                     // host-pointer calls: rows written straight into mapped host buffers
   unsigned long long device_table_cap = 0; // largest device result table (bytes) before pageable outputs
                                            // are registered and written directly; 0 = free memory less 2 GB

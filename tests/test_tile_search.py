@@ -31,7 +31,8 @@ def same(a, b):
 
 
 def join(x, k, beta, mode, tile, monkeypatch, **kw):
-    monkeypatch.setenv("KNNSJ_TILE", "1" if tile else "0")
+    # tile: True = query tiles always (3), False = off (0), or a KNNSJ_TILE value
+    monkeypatch.setenv("KNNSJ_TILE", "3" if tile is True else ("0" if tile is False else tile))
     ids, dists, st = kj.selfjoin(x, k, beta=beta, radius_mode=mode, return_stats=True, **kw)
     return (ids, dists), st
 
@@ -52,8 +53,12 @@ def test_tile_learned_equals_per_query_search(monkeypatch, d, k):
     a, st = join(x, k, 0.025, kj.RADIUS_LEARNED, True, monkeypatch)
     b, _ = join(x, k, 0.025, kj.RADIUS_LEARNED, False, monkeypatch)
     c, _ = join(x, k, 0.025, kj.RADIUS_PLAIN, True, monkeypatch)
+    e, _ = join(x, k, 0.025, kj.RADIUS_PLAIN, "2", monkeypatch)  # one warp per query, finer grid
+    f, _ = join(x, k, 0.025, kj.RADIUS_LEARNED, "2", monkeypatch)
     same(a, b)
     same(a, c)
+    same(a, e)
+    same(a, f)
 
 
 def test_tile_sky_like(monkeypatch):
@@ -75,13 +80,13 @@ def test_tile_exact_ties_are_handed_over(monkeypatch):
     same(a, (oids, odists))
 
 
-def test_tile_streamed_rows(monkeypatch):
+def test_tile_rows_into_pinned_buffers(monkeypatch):
     torch = pytest.importorskip("torch")
     n, k = 300_000, 32
     x = datasets.gmm(n, 2, 30, 0.2, 5, dtype=np.float32)
     ids = torch.empty((n, k + 1), dtype=torch.int32).pin_memory().numpy()
     dists = torch.empty((n, k + 1), dtype=torch.float32).pin_memory().numpy()
-    monkeypatch.setenv("KNNSJ_TILE", "1")
+    monkeypatch.setenv("KNNSJ_TILE", "3")
     kj.selfjoin(x, k, beta=0.025, radius_mode=kj.RADIUS_LEARNED, out_ids=ids, out_dists=dists)
     b, _ = join(x, k, 0.025, kj.RADIUS_LEARNED, False, monkeypatch)
     same((ids, dists), b)
