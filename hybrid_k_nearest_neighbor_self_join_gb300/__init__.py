@@ -177,6 +177,16 @@ def write_knn_out(directory: str, ids: np.ndarray, dists: np.ndarray) -> None:
                                                dists.ctypes.data, _dtype_code(dists.dtype)))
 
 
+def outlier_scores_device(ids_ptr: int, dists_ptr: int, dtype, n: int, K: int, mean_ptr: int, dist_rank_ptr: int,
+                          in_degree_ptr: int, degree_rank_ptr: int) -> None:
+    """Outlier scores of a device-resident result table (knnsj_outlier_scores_device);
+    all pointers are device pointers (e.g. torch.Tensor.data_ptr())."""
+    _lib.check(_lib.load().knnsj_outlier_scores_device(
+        ctypes.c_void_p(ids_ptr), ctypes.c_void_p(dists_ptr), _dtype_code(dtype), n, K, ctypes.c_void_p(mean_ptr),
+        ctypes.c_void_p(dist_rank_ptr), ctypes.c_void_p(in_degree_ptr), ctypes.c_void_p(degree_rank_ptr)),
+        "knnsj_outlier_scores_device")
+
+
 def write_outlier_scores(directory: str, ids: np.ndarray, dists: np.ndarray) -> None:
     ids = np.ascontiguousarray(ids, np.int32)
     dists = np.ascontiguousarray(dists)

@@ -169,6 +169,9 @@ _SIGNATURES = [
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     ("knnsj_write_outlier_scores", ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint64, ctypes.c_uint32,
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    ("knnsj_outlier_scores_device", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64,
+                                                   ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                                                   ctypes.c_void_p, ctypes.c_void_p]),
     ("knnsj_get_radius_model", ctypes.c_int, [ctypes.c_void_p]),
     ("knnsj_set_radius_model", ctypes.c_int, [ctypes.c_void_p]),
     ("knnsj_radius_features", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint32,

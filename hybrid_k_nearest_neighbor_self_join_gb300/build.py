@@ -31,7 +31,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp"]
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fopenmp"]
 
-CU_SOURCES = ["k_prep.cu", "k_eps.cu", "k_grid.cu", "k_search.cu", "k_tile.cu", "k_radius.cu", "k_mlp.cu", "join.cu"]
+CU_SOURCES = ["k_prep.cu", "k_eps.cu", "k_grid.cu", "k_search.cu", "k_tile.cu", "k_outlier.cu", "k_radius.cu", "k_mlp.cu", "join.cu"]
 HEADERS = ["knnsj_device.cuh", "exact_sqrt.cuh", "mlp_tc.cuh", "ring_policy.h", "knnsj_internal.h", "knnsj_host.h", "radius_model.cuh", "radius_model_weights.inc"]
 
 

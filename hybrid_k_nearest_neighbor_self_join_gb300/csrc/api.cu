@@ -807,6 +807,29 @@ knnsj_status knnsj_radius_train(const float* features, const float* targets, uin
       nullptr);
 }
 
+knnsj_status knnsj_outlier_scores_device(const int32_t* d_ids, const void* d_dists, knnsj_dtype dtype, uint64_t n,
+                                         uint32_t K, double* d_mean, int32_t* d_dist_rank, uint64_t* d_in_degree,
+                                         uint32_t* d_degree_rank) {
+  if (!d_ids || !d_dists || !d_mean || !d_dist_rank || !d_in_degree || !d_degree_rank || n == 0 || K < 2)
+    return KNNSJ_ERR_INVALID_ARGUMENT;
+  if (n >= (1ull << 31)) return KNNSJ_ERR_TOO_MANY_POINTS;
+  if (dtype != KNNSJ_F32 && dtype != KNNSJ_F64) return KNNSJ_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(g_call_mutex);
+  return guarded(
+      [&] {
+        const int dev = select_device(nullptr);
+        Workspace& w = ready_workspace(dev);
+        if (dtype == KNNSJ_F32)
+          outlier_scores_device<float>(w, d_ids, (const float*)d_dists, n, K, d_mean, d_dist_rank,
+                                       (unsigned long long*)d_in_degree, d_degree_rank, w.stream);
+        else
+          outlier_scores_device<double>(w, d_ids, (const double*)d_dists, n, K, d_mean, d_dist_rank,
+                                        (unsigned long long*)d_in_degree, d_degree_rank, w.stream);
+        KNNSJ_CUDA(cudaStreamSynchronize(w.stream));
+      },
+      nullptr);
+}
+
 void knnsj_release(void) {
   std::lock_guard<std::mutex> lock(g_call_mutex);
   int dev = 0;

@@ -330,6 +330,13 @@ size_t mlp_grad_partials(uint64_t n);  // floats of d_part for n samples
 void train_model(const float* hX, const float* hY, uint64_t n, int epochs, uint32_t batch, float lr,
                  float quantile, uint64_t seed, float* model_out, float* loss_out, cudaStream_t s);
 
+// Outlier scores of a result table on the device (k_outlier.cu): per point
+// the mean table distance and its rank (decreasing), the in-degree and its
+// rank (increasing); equal scores ranked by point id.
+template <typename T>
+void outlier_scores_device(Workspace& w, const int32_t* ids, const T* dists, uint64_t n, uint32_t K, double* mean,
+                           int32_t* dist_rank, unsigned long long* indeg, uint32_t* degree_rank, cudaStream_t s);
+
 // Verification figure of a result table on the device (synchronises s).
 template <typename T>
 double device_checksum(Workspace& w, const T* d_vals, uint64_t count, cudaStream_t s);

@@ -273,6 +273,19 @@ knnsj_status knnsj_grid_dims(const void* data, knnsj_dtype dtype, uint64_t n, ui
 knnsj_status knnsj_read_csv(const char* path, knnsj_dtype dtype, uint32_t d, void* out,
                             uint64_t* n_points);
 
+/* Outlier scores of a result table in DEVICE memory, on the GPU
+ * (printOutlierScores, main.cu:952-1067): for each point q, mean[q] = the sum
+ * of its K table distances (added in DTYPE in entry order) / (K - 1) in
+ * double; dist_rank[q] = its position by decreasing sum; in_degree[q] = the
+ * number of table entries naming q; degree_rank[q] = its position by
+ * increasing in-degree.  Equal scores are ranked by point id (the reference
+ * leaves them in std::sort's unspecified order; knnsj_write_outlier_scores
+ * keeps that order for byte-identical files).  All pointers are device
+ * pointers of the current device: ids/dists n*K, outputs n each. */
+knnsj_status knnsj_outlier_scores_device(const int32_t* d_ids, const void* d_dists, knnsj_dtype dtype,
+                                         uint64_t n, uint32_t K, double* d_mean, int32_t* d_dist_rank,
+                                         uint64_t* d_in_degree, uint32_t* d_degree_rank);
+
 /* Binary input (no reference counterpart: the reference reads CSV only,
  * import_dataset.cpp:50-106): a NumPy .npy file (format 1.0-3.0, C order,
  * little-endian float32 or float64, any shape; values converted to dtype) or,

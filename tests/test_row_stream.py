@@ -9,7 +9,8 @@
   in blocks of query ids copied out while the join runs, later passes' rows
   patched in at the end.
 Each must equal a join into ordinary pageable buffers (a device table copied
-out in one piece after the join), including the verification sum.
+out in one piece after the join) bit for bit, and its verification sum to
+rounding.
 """
 import numpy as np
 import pytest
@@ -44,6 +45,13 @@ def reference(x, k, mode, monkeypatch):
     return ref_i, ref_d, st["total_distance"]
 
 
+def close_sum(got, want):
+    # the verification sum adds each row's squared distances in float, lane
+    # partial sums first: a row finished by another kernel or pass (same
+    # values) may round differently in the last bits
+    assert abs(got - want) <= 1e-9 * abs(want), (got, want)
+
+
 def same(ids, dd, ref_i, ref_d):
     assert np.array_equal(ids, ref_i)
     bits = np.uint32 if dd.dtype == np.float32 else np.uint64
@@ -65,7 +73,7 @@ def test_direct_rows_into_pinned_buffers(monkeypatch, mode, dtype, graph):
     _, _, st = kj.selfjoin(x, k, beta=0.025, radius_mode=mode, out_ids=ids, out_dists=dd, return_stats=True)
     assert st["queries_run"] > n  # some rows were finished after the first pass
     same(ids, dd, ref_i, ref_d)
-    assert st["total_distance"] == ref_sum
+    close_sum(st["total_distance"], ref_sum)
 
 
 @pytest.mark.parametrize("mode", [kj.RADIUS_LEARNED, kj.RADIUS_PLAIN])
@@ -80,7 +88,7 @@ def test_memory_bounded_pageable_outputs(monkeypatch, mode):
     _, _, st = kj.selfjoin(x, k, beta=0.025, radius_mode=mode, out_ids=ids, out_dists=dd, return_stats=True,
                            device_table_mb=1)
     same(ids, dd, ref_i, ref_d)
-    assert st["total_distance"] == ref_sum
+    close_sum(st["total_distance"], ref_sum)
 
 
 @pytest.mark.parametrize("mode,chunks,graph", [(kj.RADIUS_LEARNED, "8", "1"), (kj.RADIUS_PLAIN, "3", "0")])
@@ -97,6 +105,4 @@ def test_streamed_rows_match_one_copy(monkeypatch, mode, chunks, graph):
     dd[:] = np.nan
     _, _, st = kj.selfjoin(x, k, beta=0.025, radius_mode=mode, out_ids=ids, out_dists=dd, return_stats=True)
     same(ids, dd, ref_i, ref_d)
-    # (rows may be written by the other search kernel here, whose per-row sum
-    # adds the same values in another order)
-    assert abs(st["total_distance"] - ref_sum) <= 1e-6 * abs(ref_sum)
+    close_sum(st["total_distance"], ref_sum)
