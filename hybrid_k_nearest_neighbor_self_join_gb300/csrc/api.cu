@@ -157,17 +157,17 @@ void init_stats(knnsj_stats* st) {
 }
 
 // Where the rows of a host-pointer call go:
-//  * direct rows (default): when both output buffers are pinned and mapped
-//    into the device's address space, the search kernels write every row
-//    straight into them (no device result table, no copy after the join);
-//  * when the device result table would not fit (more than the free device
-//    memory less a margin, or cfg.device_table_cap), pageable output buffers
-//    are registered with the device for the duration of the call and take
-//    their rows the same way -- the device then holds no result table at
-//    all, which bounds device memory by the input and the index;
-//  * otherwise a device result table, copied out after the join (or streamed
-//    out in blocks of query ids while the join runs, cfg.row_chunks >= 2 with
-//    direct rows off).
+//  * a device result table whose rows are streamed into pinned output
+//    buffers in blocks of query ids while the join runs (n >= 2^18,
+//    cfg.row_chunks >= 2), or copied out after the join;
+//  * direct rows: when the device result table would not fit (more than the
+//    free device memory less a margin, or cfg.device_table_cap) -- or with
+//    cfg.direct_rows for pinned outputs -- the search kernels write every
+//    row straight into the host buffers, pageable ones being registered with
+//    the device for the duration of the call; the device then holds no
+//    result table at all, which bounds device memory by the input and the
+//    index.  (Measured on the 25M-point sky-like join: 130 ms per join with
+//    direct rows, 86 ms streamed, 133 ms with one copy after the join.)
 constexpr uint64_t ROW_STREAM_MIN_ROWS = 1u << 18;
 
 // Device-visible address of a host buffer, when it is pinned and mapped.
@@ -226,21 +226,24 @@ void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t 
   T* d_dev = nullptr;
   HostRegistration reg;
   reg.stream = s;
-  if (cfg.direct_rows) {
-    ids_dev = (int32_t*)mapped_host_pointer(out_ids);
-    d_dev = (T*)mapped_host_pointer(out_d);
-    if (!ids_dev || !d_dev) {
-      ids_dev = nullptr;
-      d_dev = nullptr;
-      size_t free_b = 0, total_b = 0;
-      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) cudaGetLastError();
-      const uint64_t cap = cfg.device_table_cap ? cfg.device_table_cap
-                                                : (free_b > (2ull << 30) ? (uint64_t)free_b - (2ull << 30) : 0ull);
-      if (table_bytes > cap && reg.add(out_ids, n * K * 4) && reg.add(out_d, n * K * sizeof(T))) {
-        ids_dev = (int32_t*)mapped_host_pointer(out_ids);
-        d_dev = (T*)mapped_host_pointer(out_d);
-        if (!ids_dev || !d_dev) ids_dev = nullptr, d_dev = nullptr;
-      }
+  {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) cudaGetLastError();
+    const uint64_t cap = cfg.device_table_cap ? cfg.device_table_cap
+                                              : (free_b > (2ull << 30) ? (uint64_t)free_b - (2ull << 30) : 0ull);
+    const bool fits = table_bytes <= cap;
+    int32_t* mi = (int32_t*)mapped_host_pointer(out_ids);
+    T* md = (T*)mapped_host_pointer(out_d);
+    const bool pinned = mi && md;
+    // pinned: direct rows when asked for or when the table does not fit;
+    // otherwise streamed (large) or one copy (small) from a device table
+    if (pinned && (cfg.direct_rows == 1 || !fits)) {
+      ids_dev = mi;
+      d_dev = md;
+    } else if (!pinned && !fits && reg.add(out_ids, n * K * 4) && reg.add(out_d, n * K * sizeof(T))) {
+      ids_dev = (int32_t*)mapped_host_pointer(out_ids);
+      d_dev = (T*)mapped_host_pointer(out_d);
+      if (!ids_dev || !d_dev) ids_dev = nullptr, d_dev = nullptr;
     }
   }
   if (ids_dev && d_dev) {

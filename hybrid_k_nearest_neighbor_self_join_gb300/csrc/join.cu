@@ -833,11 +833,13 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
   // 5b. the first pass's tile search (2-D / 3-D float data, all indexed)
   TileSetup<T> tile;
   const bool will_stream = rows && rows->chunks >= 2 && n >= (uint64_t)rows->chunks;
-  if (cfg.tile_search && !will_stream && tile_search_applies(d, di, K, P.grid.dense, sizeof(T))) {
+  if (cfg.tile_search && tile_search_applies(d, di, K, P.grid.dense, sizeof(T))) {
     // per-query starting radii: query tiles over a grid of width eps0/4; a
     // uniform radius: one warp per query over a grid of width eps0/2
-    // (measured best for each on the 25M-point sky-like set)
-    const bool tiles = cfg.tile_search == 3 || (cfg.tile_search == 1 && qrad != nullptr);
+    // (measured best for each on the 25M-point sky-like set).  Streamed rows
+    // search blocks of query ids, spread over the whole dataset: one warp
+    // per query there.
+    const bool tiles = !will_stream && (cfg.tile_search == 3 || (cfg.tile_search == 1 && qrad != nullptr));
     const int fine = cfg.tile_fine > 0 ? cfg.tile_fine : (tiles ? 4 : 2);
     prepare_tile<T>(w, tiles, fine, P.grid, P.xs, n, d, P.eps0, P.mx, &tile, s);
   }
@@ -932,8 +934,10 @@ void run_join(Workspace& w, const JoinConfig& cfg, const T* d_aos, const T* h_ao
       a.qlist = clist + r0;
       a.nq = (uint32_t)nr;
       // (the queries of a block of ids are spread over the whole dataset:
-      // the per-query search, not query tiles)
-      launch_search<T>(a, w.sm_count, s);
+      // the per-query search, over the finer grid when one is set up)
+      SearchLaunch<T> c = a;
+      if (tile.on) c.grid = tile.cand;
+      launch_search<T>(c, w.sm_count, s);
       KNNSJ_CUDA(cudaEventRecord(w.chunk_ev[ch], s));
       KNNSJ_CUDA(cudaStreamWaitEvent(w.copy_stream, w.chunk_ev[ch], 0));
       KNNSJ_CUDA(cudaMemcpyAsync((int32_t*)rows->ids_host + r0 * K, d_ids + r0 * K, nr * K * 4,

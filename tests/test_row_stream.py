@@ -1,13 +1,12 @@
 """Where the rows of host-pointer joins go, and that they are the same rows.
 
-* pinned, mapped output buffers: the search kernels write every row straight
-  into them (no device result table, no copy after the join);
+* pinned output buffers (default): rows in blocks of query ids copied out
+  while the join runs, later passes' rows patched in at the end;
+* pinned buffers with direct rows (KNNSJ_DIRECT_ROWS=1): the search kernels
+  write every row straight into them (no device result table, no copy);
 * pageable buffers whose result table is larger than the device-table cap
   (opts->device_table_mb, the memory-bounded mode): the buffers are registered
-  with the device for the call and written the same way;
-* with direct rows off (KNNSJ_DIRECT_ROWS=0), pinned buffers take their rows
-  in blocks of query ids copied out while the join runs, later passes' rows
-  patched in at the end.
+  with the device for the call and written directly.
 Each must equal a join into ordinary pageable buffers (a device table copied
 out in one piece after the join) bit for bit, and its verification sum to
 rounding.
@@ -66,6 +65,7 @@ def test_direct_rows_into_pinned_buffers(monkeypatch, mode, dtype, graph):
     x = datasets.sky_like(n, seed=31).astype(dtype)
     ref_i, ref_d, ref_sum = reference(x, k, mode, monkeypatch)
     monkeypatch.setenv("KNNSJ_GRAPH", graph)
+    monkeypatch.setenv("KNNSJ_DIRECT_ROWS", "1")
     t_i, ids = pinned((n, k + 1), np.int32)
     t_d, dd = pinned((n, k + 1), dtype)
     ids[:] = -7
@@ -96,7 +96,6 @@ def test_streamed_rows_match_one_copy(monkeypatch, mode, chunks, graph):
     n, k = 400_000, 32
     x = datasets.sky_like(n, seed=31)
     ref_i, ref_d, ref_sum = reference(x, k, mode, monkeypatch)
-    monkeypatch.setenv("KNNSJ_DIRECT_ROWS", "0")
     monkeypatch.setenv("KNNSJ_ROW_CHUNKS", chunks)
     monkeypatch.setenv("KNNSJ_GRAPH", graph)
     t_i, ids = pinned((n, k + 1), np.int32)
