@@ -157,17 +157,20 @@ void init_stats(knnsj_stats* st) {
 }
 
 // Where the rows of a host-pointer call go:
-//  * a device result table whose rows are streamed into pinned output
-//    buffers in blocks of query ids while the join runs (n >= 2^18,
-//    cfg.row_chunks >= 2), or copied out after the join;
-//  * direct rows: when the device result table would not fit (more than the
-//    free device memory less a margin, or cfg.device_table_cap) -- or with
-//    cfg.direct_rows for pinned outputs -- the search kernels write every
-//    row straight into the host buffers, pageable ones being registered with
-//    the device for the duration of the call; the device then holds no
+//  * direct rows: pinned output buffers (cfg.direct_rows, the default), and
+//    any outputs whose device result table would not fit (more than the
+//    free device memory less a margin, or cfg.device_table_cap), take every
+//    row straight from the search kernels, pageable ones being registered
+//    with the device for the duration of the call; the device then holds no
 //    result table at all, which bounds device memory by the input and the
-//    index.  (Measured on the 25M-point sky-like join: 130 ms per join with
-//    direct rows, 86 ms streamed, 133 ms with one copy after the join.)
+//    index;
+//  * otherwise a device result table whose rows are streamed into pinned
+//    buffers in blocks of query ids while the join runs (cfg.direct_rows 0,
+//    n >= 2^18, cfg.row_chunks >= 2), or copied out after the join.
+// Measured on the 25M-point sky-like join (13 GB of rows): direct rows
+// 128-132 ms per join on every box tried; streamed 86-89 ms on some boxes,
+// but 150-350 ms steps on others, where the copy engines' device-to-host
+// rate fell to ~50 GB/s for seconds at a time; one copy after the join 133 ms.
 constexpr uint64_t ROW_STREAM_MIN_ROWS = 1u << 18;
 
 // Device-visible address of a host buffer, when it is pinned and mapped.
@@ -235,8 +238,8 @@ void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t 
     int32_t* mi = (int32_t*)mapped_host_pointer(out_ids);
     T* md = (T*)mapped_host_pointer(out_d);
     const bool pinned = mi && md;
-    // pinned: direct rows when asked for or when the table does not fit;
-    // otherwise streamed (large) or one copy (small) from a device table
+    // pinned: direct rows unless turned off (and then still when the table
+    // does not fit); otherwise streamed (large) or one copy (small)
     if (pinned && (cfg.direct_rows == 1 || !fits)) {
       ids_dev = mi;
       d_dev = md;

@@ -40,8 +40,8 @@ struct JoinConfig {
                                            // per query for a uniform radius, 2 always one warp per query,
                                            // 3 always query tiles
   int tile_fine = 0;                       // that grid's cells: eps0 / tile_fine (0: 4 for tiles, 2 else)
-  int direct_rows = 0;                     // 1: pinned outputs take their rows straight from the kernels
-                                           // (otherwise only when the device table does not fit)
+  int direct_rows = 1;                     // pinned outputs take their rows straight from the kernels
+                                           // (0: streamed from a device table by the copy engines)
   unsigned long long device_table_cap = 0; // largest device result table (bytes) before pageable outputs
                                            // are registered and written directly; 0 = free memory less 2 GB
 };

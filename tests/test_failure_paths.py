@@ -2,9 +2,10 @@
 
 * KNNSJ_ERR_NO_CONVERGENCE: an iteration cap (max_iterations=1) on a join
   that needs several passes, through the host-driven retry loop, the loop in
-  a CUDA graph and the streamed-rows path; the call returns the status, no
-  copy into the caller's buffers is left in flight, and the library keeps
-  working afterwards.
+  a CUDA graph, and pinned outputs (rows written by the kernels, or streamed
+  by copies); the call returns the status, no kernel or copy writing into
+  the caller's buffers is left in flight, and the library keeps working
+  afterwards.
 * The tensor-core radius model's bounded mbarrier waits: with the test
   switch KNNSJ_TEST_MLP_TIMEOUT=1 the MLP issues no MMA (nothing is in
   flight) and waits only briefly, so every tile takes the timeout path; the
@@ -52,9 +53,13 @@ def test_iteration_cap_reports_no_convergence(monkeypatch, graph):
     assert np.array_equal(dists.view(np.uint32), odists.view(np.uint32))
 
 
-def test_iteration_cap_with_streamed_rows_leaves_no_copy_in_flight():
+@pytest.mark.parametrize("direct", ["1", "0"])
+def test_iteration_cap_with_pinned_outputs_leaves_nothing_in_flight(monkeypatch, direct):
+    # direct "1": rows written by the kernels into the pinned buffers;
+    # "0": rows streamed out of a device table by copies
+    monkeypatch.setenv("KNNSJ_DIRECT_ROWS", direct)
     torch = pytest.importorskip("torch")
-    n, k = 300_000, 8  # >= 2^18 rows: pinned outputs are streamed during the join
+    n, k = 300_000, 8  # >= 2^18 rows: with direct "0" the rows are streamed during the join
     x = datasets.uniform(n, 2, 6)
     ids = torch.full((n, k + 1), -3, dtype=torch.int32).pin_memory().numpy()
     dists = torch.full((n, k + 1), -3.0, dtype=torch.float32).pin_memory().numpy()

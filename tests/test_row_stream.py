@@ -1,9 +1,9 @@
 """Where the rows of host-pointer joins go, and that they are the same rows.
 
-* pinned output buffers (default): rows in blocks of query ids copied out
-  while the join runs, later passes' rows patched in at the end;
-* pinned buffers with direct rows (KNNSJ_DIRECT_ROWS=1): the search kernels
-  write every row straight into them (no device result table, no copy);
+* pinned output buffers (default): the search kernels write every row
+  straight into them (no device result table, no copy);
+* pinned buffers with KNNSJ_DIRECT_ROWS=0: rows in blocks of query ids
+  copied out while the join runs, later passes' rows patched in at the end;
 * pageable buffers whose result table is larger than the device-table cap
   (opts->device_table_mb, the memory-bounded mode): the buffers are registered
   with the device for the call and written directly.
@@ -96,6 +96,7 @@ def test_streamed_rows_match_one_copy(monkeypatch, mode, chunks, graph):
     n, k = 400_000, 32
     x = datasets.sky_like(n, seed=31)
     ref_i, ref_d, ref_sum = reference(x, k, mode, monkeypatch)
+    monkeypatch.setenv("KNNSJ_DIRECT_ROWS", "0")
     monkeypatch.setenv("KNNSJ_ROW_CHUNKS", chunks)
     monkeypatch.setenv("KNNSJ_GRAPH", graph)
     t_i, ids = pinned((n, k + 1), np.int32)
