@@ -511,7 +511,8 @@ static void prepare_tile(Workspace& w, bool tiles, int fine_max, const DeviceGri
     uint32_t* tmp = (uint32_t*)w.scan_tmp.get(std::max(sc.scan_tmp_elems, scan_tmp_elems(mult)) * 4);
     T* fps = (T*)w.fps.get(n * d * sizeof(T));
     uint32_t* fpid = (uint32_t*)w.fpid.get(n * 4);
-    launch_counting_grid<T>(xs, n, d, gf, tbl, tmp, fps, fpid, s);
+    // (points visited in eps0-cell order: neighbours fall in the same cells)
+    launch_counting_grid<T>(g.ps, g.pid, n, d, gf, tbl, tmp, fps, fpid, s);
     t->cand.geom = gf;
     t->cand.ps = fps;
     t->cand.psf = nullptr;

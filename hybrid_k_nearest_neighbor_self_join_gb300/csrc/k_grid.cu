@@ -293,16 +293,30 @@ __global__ void morton_key_kernel(const T* __restrict__ ps, uint64_t n, const Gr
 }
 
 // Counting sort of points into the cells of a grid (any order within a
-// cell): tbl[L + 1] counts cell L, ...
+// cell).  The points are visited in the order of src (cell-ordered columns of
+// a coarser grid keep neighbours together), and the lanes of a warp that
+// fall in one cell take their counts or positions with one atomic:
+// tbl[L + 1] counts cell L, ...
 template <typename T>
-__global__ void cell_count_atomic_kernel(const T* __restrict__ xs, uint64_t n, const GridGeom<T> g,
+__device__ __forceinline__ unsigned long long cell_of(const T* __restrict__ src, uint64_t n, uint64_t i,
+                                                      const GridGeom<T>& g) {
+  unsigned long long lin = 0;
+  for (uint32_t j = 0; j < g.di; j++)
+    lin += (unsigned long long)point_cell_coord(src[(uint64_t)j * n + i], g.minv[j], g.width) * g.mult[j];
+  return lin;
+}
+
+template <typename T>
+__global__ void cell_count_atomic_kernel(const T* __restrict__ src, uint64_t n, const GridGeom<T> g,
                                          uint32_t* __restrict__ tbl) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    unsigned long long lin = 0;
-    for (uint32_t j = 0; j < g.di; j++)
-      lin += (unsigned long long)point_cell_coord(xs[(uint64_t)j * n + i], g.minv[j], g.width) * g.mult[j];
-    atomicAdd(&tbl[lin + 1], 1u);
+  const int lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint64_t i = base + threadIdx.x;
+    const bool live = i < n;
+    const unsigned long long lin = live ? cell_of(src, n, i, g) : ~0ull;
+    const unsigned peers = __match_any_sync(FULL, lin);
+    if (live && lane == __ffs(peers) - 1) atomicAdd(&tbl[lin + 1], (uint32_t)__popc(peers));
   }
 }
 
@@ -310,17 +324,25 @@ __global__ void cell_count_atomic_kernel(const T* __restrict__ xs, uint64_t n, c
 // each point takes the next position of its cell (leaving tbl[L + 1] at the
 // cell's end, which is where cell L + 1 starts: tbl becomes the start table).
 template <typename T>
-__global__ void cell_scatter_atomic_kernel(const T* __restrict__ xs, uint64_t n, uint32_t d, const GridGeom<T> g,
-                                           uint32_t* __restrict__ tbl, T* __restrict__ ps,
-                                           uint32_t* __restrict__ pid) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    unsigned long long lin = 0;
-    for (uint32_t j = 0; j < g.di; j++)
-      lin += (unsigned long long)point_cell_coord(xs[(uint64_t)j * n + i], g.minv[j], g.width) * g.mult[j];
-    const uint32_t pos = atomicAdd(&tbl[lin + 1], 1u);
-    for (uint32_t j = 0; j < d; j++) ps[(uint64_t)j * n + pos] = xs[(uint64_t)j * n + i];
-    pid[pos] = (uint32_t)i;
+__global__ void cell_scatter_atomic_kernel(const T* __restrict__ src, const uint32_t* __restrict__ src_ids, uint64_t n,
+                                           uint32_t d, const GridGeom<T> g, uint32_t* __restrict__ tbl,
+                                           T* __restrict__ ps, uint32_t* __restrict__ pid) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t b0 = (uint64_t)blockIdx.x * blockDim.x; b0 < n; b0 += stride) {
+    const uint64_t i = b0 + threadIdx.x;
+    const bool live = i < n;
+    const unsigned long long lin = live ? cell_of(src, n, i, g) : ~0ull;
+    const unsigned peers = __match_any_sync(FULL, lin);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (live && lane == leader) base = atomicAdd(&tbl[lin + 1], (uint32_t)__popc(peers));
+    base = __shfl_sync(FULL, base, leader);
+    if (live) {
+      const uint32_t pos = base + __popc(peers & lanemask_lt());
+      for (uint32_t j = 0; j < d; j++) ps[(uint64_t)j * n + pos] = src[(uint64_t)j * n + i];
+      pid[pos] = src_ids ? src_ids[i] : (uint32_t)i;
+    }
   }
 }
 
@@ -397,13 +419,13 @@ void launch_morton_keys(const T* ps, uint64_t n, const GridGeom<T>& g, int bits,
 }
 
 template <typename T>
-void launch_counting_grid(const T* xs, uint64_t n, uint32_t d, const GridGeom<T>& g, uint32_t* tbl,
-                          uint32_t* scan_tmp, T* ps, uint32_t* pid, cudaStream_t s) {
+void launch_counting_grid(const T* src, const uint32_t* src_ids, uint64_t n, uint32_t d, const GridGeom<T>& g,
+                          uint32_t* tbl, uint32_t* scan_tmp, T* ps, uint32_t* pid, cudaStream_t s) {
   launch_zero_words(tbl, (g.total_cells + 1) * 4, s);
-  cell_count_atomic_kernel<T><<<grid_blocks(n), 256, 0, s>>>(xs, n, g, tbl);
+  cell_count_atomic_kernel<T><<<grid_blocks(n), 256, 0, s>>>(src, n, g, tbl);
   KNNSJ_CHECK_LAUNCH();
   scan_exclusive_u32(tbl + 1, tbl + 1, g.total_cells, scan_tmp, s);
-  cell_scatter_atomic_kernel<T><<<grid_blocks(n), 256, 0, s>>>(xs, n, d, g, tbl, ps, pid);
+  cell_scatter_atomic_kernel<T><<<grid_blocks(n), 256, 0, s>>>(src, src_ids, n, d, g, tbl, ps, pid);
   KNNSJ_CHECK_LAUNCH();
 }
 
@@ -422,10 +444,10 @@ template void launch_morton_keys<float>(const float*, uint64_t, const GridGeom<f
                                         uint32_t*, cudaStream_t);
 template void launch_morton_keys<double>(const double*, uint64_t, const GridGeom<double>&, int,
                                          unsigned long long*, uint32_t*, cudaStream_t);
-template void launch_counting_grid<float>(const float*, uint64_t, uint32_t, const GridGeom<float>&, uint32_t*,
-                                          uint32_t*, float*, uint32_t*, cudaStream_t);
-template void launch_counting_grid<double>(const double*, uint64_t, uint32_t, const GridGeom<double>&, uint32_t*,
-                                           uint32_t*, double*, uint32_t*, cudaStream_t);
+template void launch_counting_grid<float>(const float*, const uint32_t*, uint64_t, uint32_t, const GridGeom<float>&,
+                                          uint32_t*, uint32_t*, float*, uint32_t*, cudaStream_t);
+template void launch_counting_grid<double>(const double*, const uint32_t*, uint64_t, uint32_t, const GridGeom<double>&,
+                                           uint32_t*, uint32_t*, double*, uint32_t*, cudaStream_t);
 template void launch_gather_sorted<float>(const float*, uint64_t, uint32_t, const uint32_t*, float*, float*,
                                           cudaStream_t);
 template void launch_gather_sorted<double>(const double*, uint64_t, uint32_t, const uint32_t*, double*, float*,

@@ -136,10 +136,11 @@ void launch_morton_keys(const T* ps, uint64_t n, const GridGeom<T>& g, int bits,
                         uint32_t* vals, cudaStream_t s);
 // Grid by counting sort (points in any order within a cell): tbl (total+1
 // entries) becomes the dense start table, ps/pid the cell-ordered columns and
-// ids of the input-order columns xs.  scan_tmp: scan_tmp_elems(total).
+// ids of the points given as columns src with ids src_ids (null: 0, 1, ...).
+// scan_tmp: scan_tmp_elems(total).
 template <typename T>
-void launch_counting_grid(const T* xs, uint64_t n, uint32_t d, const GridGeom<T>& g, uint32_t* tbl,
-                          uint32_t* scan_tmp, T* ps, uint32_t* pid, cudaStream_t s);
+void launch_counting_grid(const T* src, const uint32_t* src_ids, uint64_t n, uint32_t d, const GridGeom<T>& g,
+                          uint32_t* tbl, uint32_t* scan_tmp, T* ps, uint32_t* pid, cudaStream_t s);
 template <typename T>
 // psf (optional): the same columns rounded to float (double data: the
 // search's float prefilter)
