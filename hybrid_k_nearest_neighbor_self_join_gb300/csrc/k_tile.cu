@@ -208,15 +208,15 @@ __global__ void __launch_bounds__(TILE_THREADS, 5) tile_kernel(const TileParams 
       LO[j] = __reduce_min_sync(FULL, in ? lo[j] : 0xffffffffu);
       HI[j] = __reduce_max_sync(FULL, in ? hi[j] : 0u);
     }
-    const uint32_t ext1 = HI[1] - LO[1] + 1;
-    const uint32_t ext2 = D == 3 ? HI[D - 1] - LO[D - 1] + 1 : 1u;
+    uint32_t ext1 = HI[1] - LO[1] + 1;
+    uint32_t ext2 = D == 3 ? HI[D - 1] - LO[D - 1] + 1 : 1u;
     uint64_t nrows64 = __ballot_sync(FULL, in) ? (uint64_t)ext1 * ext2 : 0;
     if (nrows64 > TILE_MAX_ROWS) {  // (uniform) the whole tile goes to search_kernel
       defer = valid;
       in = false;
       nrows64 = 0;
     }
-    const uint32_t nrows = (uint32_t)nrows64;
+    uint32_t nrows = (uint32_t)nrows64;
     warp_append(defer && lead, qid, p.defer_list, p.defer_count, lane);
 
     const float thr = in ? within_threshold(r) : -1.0f;  // acc <= thr never holds off the tile
@@ -379,6 +379,36 @@ __global__ void __launch_bounds__(TILE_THREADS, 5) tile_kernel(const TileParams 
     uint32_t found = 0, c_lo = 0, m = 0, bs0 = TILE_BINS;
     walk_bins(hq, 0u, true, found, c_lo, m, bs0);
     bool ok = in && found >= K;
+    // Only keys in bins up to the boundary bin are wanted from here on: a
+    // key of bin <= bs0 has acc * s0 < bs0 + 1/2 (the bin is acc * s0
+    // rounded to nearest), so its point lies within radius
+    // sqrt((bs0 + 1/2) / s0), widened here by 2^-10; the refinement passes
+    // and pass 2 scan the union of the accepted queries' rings at that
+    // radius (the boundary bin sits near the middle of the radius' range of
+    // squared distances, so the box is about half as large).
+    {
+      float rp = 0.0f;
+      if (ok && bs0 < (uint32_t)TILE_BINS - 1 && s0 > 0.0f)
+        rp = fminf(sqrtf(((float)bs0 + 0.5f) / s0 * (1.0f + 1.0f / 1048576.0f)) * (1.0f + 1.0f / 1024.0f), r);
+      else if (ok)
+        rp = r;
+      const float rpf = rp * (1.0f + 1.0f / 8192.0f);
+#pragma unroll
+      for (int j = 0; j < D; j++) {
+        const float slack = (fabsf(q[j]) + rpf) * (1.0f / 2097152.0f);
+        const uint32_t l2 = ring_cell(q[j] - rpf - slack, s_minf[j], s_invw, p.g.ncell[j], false);
+        const uint32_t h2 = ring_cell(q[j] + rpf + slack, s_minf[j], s_invw, p.g.ncell[j], true);
+        LO[j] = __reduce_min_sync(FULL, ok ? l2 : 0xffffffffu);
+        HI[j] = __reduce_max_sync(FULL, ok ? h2 : 0u);
+      }
+      if (__any_sync(FULL, ok)) {
+        ext1 = HI[1] - LO[1] + 1;
+        ext2 = D == 3 ? HI[D - 1] - LO[D - 1] + 1 : 1u;
+        nrows = ext1 * ext2;  // (within the first box: at most TILE_MAX_ROWS)
+      } else {
+        nrows = 0;
+      }
+    }
     // refinement of the boundary bin while it overflows the overflow list
     int lev = 0;
     int bs[3] = {(int)bs0, TILE_BINS, TILE_BINS};
