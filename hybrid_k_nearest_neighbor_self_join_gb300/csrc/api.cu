@@ -157,20 +157,27 @@ void init_stats(knnsj_stats* st) {
 }
 
 // Where the rows of a host-pointer call go:
-//  * direct rows: pinned output buffers (cfg.direct_rows, the default), and
-//    any outputs whose device result table would not fit (more than the
-//    free device memory less a margin, or cfg.device_table_cap), take every
-//    row straight from the search kernels, pageable ones being registered
-//    with the device for the duration of the call; the device then holds no
+//  * pinned output buffers (cfg.direct_rows 2, the default): a device
+//    result table, copied into them after the join by an SM kernel through
+//    their mapped addresses (whole cache lines in address order);
+//  * direct rows: pinned buffers with cfg.direct_rows 1, and any outputs
+//    whose device result table would not fit (more than the free device
+//    memory less a margin, or cfg.device_table_cap), take every row
+//    straight from the search kernels, pageable ones being registered with
+//    the device for the duration of the call; the device then holds no
 //    result table at all, which bounds device memory by the input and the
 //    index;
 //  * otherwise a device result table whose rows are streamed into pinned
-//    buffers in blocks of query ids while the join runs (cfg.direct_rows 0,
-//    n >= 2^18, cfg.row_chunks >= 2), or copied out after the join.
-// Measured on the 25M-point sky-like join (13 GB of rows): direct rows
-// 128-132 ms per join on every box tried; streamed 86-89 ms on some boxes,
-// but 150-350 ms steps on others, where the copy engines' device-to-host
-// rate fell to ~50 GB/s for seconds at a time; one copy after the join 133 ms.
+//    buffers by the copy engines in blocks of query ids while the join runs
+//    (cfg.direct_rows 0, n >= 2^18, cfg.row_chunks >= 2), or copied out
+//    after the join.
+// Measured on the 25M-point sky-like join (13 GB of rows) with the query-tile
+// first pass: the SM copy after the join 116 ms per join (37 ms search, 67 ms
+// copy, the link's rate); direct rows 149 ms (rows land in scattered 260-byte
+// pieces, partial cache lines); streamed 86 ms on some boxes, but 150-350 ms
+// steps on others, where the copy engines' device-to-host rate fell to
+// ~50 GB/s for seconds at a time (the SM writes of direct rows were steady
+// there).
 constexpr uint64_t ROW_STREAM_MIN_ROWS = 1u << 18;
 
 // Device-visible address of a host buffer, when it is pinned and mapped.
@@ -229,17 +236,17 @@ void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t 
   T* d_dev = nullptr;
   HostRegistration reg;
   reg.stream = s;
+  int32_t* mi = (int32_t*)mapped_host_pointer(out_ids);
+  T* md = (T*)mapped_host_pointer(out_d);
+  const bool pinned = mi && md;
   {
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) cudaGetLastError();
     const uint64_t cap = cfg.device_table_cap ? cfg.device_table_cap
                                               : (free_b > (2ull << 30) ? (uint64_t)free_b - (2ull << 30) : 0ull);
     const bool fits = table_bytes <= cap;
-    int32_t* mi = (int32_t*)mapped_host_pointer(out_ids);
-    T* md = (T*)mapped_host_pointer(out_d);
-    const bool pinned = mi && md;
-    // pinned: direct rows unless turned off (and then still when the table
-    // does not fit); otherwise streamed (large) or one copy (small)
+    // pinned: direct rows when asked for or when the table does not fit;
+    // otherwise a device table (below)
     if (pinned && (cfg.direct_rows == 1 || !fits)) {
       ids_dev = mi;
       d_dev = md;
@@ -270,7 +277,7 @@ void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t 
   T* ddist = (T*)w.dists.get(n * K * sizeof(T));
   RowStream rs;
   RowStream* rsp = nullptr;
-  if (cfg.row_chunks >= 2 && n >= ROW_STREAM_MIN_ROWS) {
+  if (cfg.direct_rows == 0 && cfg.row_chunks >= 2 && n >= ROW_STREAM_MIN_ROWS) {
     cudaPointerAttributes ai{}, ad{};
     if (cudaPointerGetAttributes(&ai, out_ids) == cudaSuccess && cudaPointerGetAttributes(&ad, out_d) == cudaSuccess &&
         ai.type == cudaMemoryTypeHost && ad.type == cudaMemoryTypeHost && ai.devicePointer && ad.devicePointer) {
@@ -298,7 +305,10 @@ void host_join_ws(Workspace& w, const T* data, uint64_t n, uint32_t d, uint32_t 
   KNNSJ_CUDA(cudaEventCreate(&t2));
   KNNSJ_CUDA(cudaEventCreate(&t3));
   KNNSJ_CUDA(cudaEventRecord(t2, s));
-  if (!streamed) {
+  if (!streamed && pinned && cfg.direct_rows == 2) {
+    launch_copy_to_mapped(mi, dids, n * K * 4, w.sm_count, s);
+    launch_copy_to_mapped(md, ddist, n * K * sizeof(T), w.sm_count, s);
+  } else if (!streamed) {
     KNNSJ_CUDA(cudaMemcpyAsync(out_ids, dids, n * K * 4, cudaMemcpyDeviceToHost, s));
     KNNSJ_CUDA(cudaMemcpyAsync(out_d, ddist, n * K * sizeof(T), cudaMemcpyDeviceToHost, s));
   }

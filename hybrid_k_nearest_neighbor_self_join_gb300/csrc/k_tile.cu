@@ -1,7 +1,7 @@
 // k_tile.cu -- range search of low-dimensional float data by tiles of
-// queries: one warp owns up to 32 queries that are neighbours in cell order,
-// one lane per query, and the tile's queries share one pass over the
-// candidates of the union of their cell rings.
+// queries: one warp owns QPT queries (4 by default) that are neighbours in
+// Morton order of their cells, 32 / QPT lanes per query, and the tile's
+// queries share one pass over the candidates of the union of their rings.
 //
 // Replaces, for the first search pass of float data with two or three
 // dimensions (all indexed) and k+1 <= 65, the same reference steps as
@@ -11,29 +11,33 @@
 // storeNeighborTableForkNNOnTheFly (GPU.cu:3610-3704).
 //
 // Per tile (one warp):
-//   1. every lane computes its query's cell ring, the warp takes the union
-//      box (lanes whose ring is much wider than the tile's median are handed
-//      to search_kernel instead, so one outlier does not widen everyone's
-//      scan); each ring row of the box (consecutive cells along dimension 0)
-//      is one contiguous run of the cell-ordered columns;
-//   2. candidates are staged in shared memory 64 at a time (coalesced
-//      loads: coordinates and id in one 16-byte record) and read back by every
-//      lane at once (broadcast);
-//   3. pass 1: each lane counts its candidates within its own radius in 32
-//      bins of squared distance (a monotone map of [0, r^2]): the bin holding
-//      the K-th smallest, the count below it, and whether the query can be
-//      accepted (at least K points within r, the reference's rule,
-//      GPU.cu:3659-3669);
-//      when the boundary bin holds more keys than the overflow area, a
-//      refinement pass splits that bin 32 ways (at most two refinements;
-//      beyond, the query goes to search_kernel: only exact ties get there);
-//   4. pass 2: keys below the boundary bin are placed at their bin's running
-//      position in the lane's row (a counting sort by bin), keys of the
-//      boundary bin go to a small per-lane overflow list;
-//   5. each lane insertion-sorts its row (bins are already in order, so this
-//      only orders keys within a bin), sorts the overflow list and completes
-//      the row with its smallest keys; the warp then writes the 32 rows with
-//      coalesced stores, distances as sqrt in the data type.
+//   1. each query's cell ring, the union box of the tile's rings (a query
+//      whose ring is much wider than the tile's mean is handed to
+//      search_kernel instead, so one outlier does not widen everyone's
+//      scan); each row of the box (consecutive cells along dimension 0) is
+//      one contiguous run of the cell-ordered columns;
+//   2. the box's candidates are staged in shared memory 64 at a time
+//      (coalesced loads: coordinates and id in one 16-byte record, the next
+//      chunk in flight while the current one is evaluated); lane (slot q,
+//      phase p) evaluates candidates p, p + 32 / QPT, ... for query q;
+//   3. the single pass over the candidates: every key (squared distance,
+//      id) within the query's radius goes to the query's list in shared
+//      memory, its slot from a ballot over the query's lanes (no atomics);
+//      a query that finds more keys than the list holds (about 1 %) is
+//      handed to search_kernel, one that finds fewer than K fails (the
+//      reference's acceptance rule, GPU.cu:3659-3669);
+//   4. a histogram of the list in 128 bins of squared distance (a monotone
+//      map of [0, r^2]; 8-bit counts, four to a word, scanned bytewise),
+//      the bin holding the K-th smallest key and the count below it; a
+//      boundary bin with more keys than the 16-entry overflow list is split
+//      32 ways (at most two refinements; beyond, only exact ties, the query
+//      goes to search_kernel);
+//   5. placement: the list index of every key below the boundary bin goes
+//      to its bin's running slot of the row (a counting sort by bin), keys
+//      of the boundary bin to the overflow list; the few bins holding two
+//      keys or more are sorted, and so is the overflow list;
+//   6. the warp writes each query's row with coalesced stores (distances
+//      as sqrt in the data type), the first K - c_lo overflow keys last.
 // Squared distances use the reference's fma chain in dimension order
 // (kernel.cu:139-140) exactly as search_kernel does, so rows are identical.
 // Keys are (squared distance bits, id) in one u64: ties are ordered by id.
@@ -50,9 +54,9 @@ namespace {
 constexpr int TILE_WARPS = 4;                    // warps per block
 constexpr int TILE_THREADS = TILE_WARPS * 32;
 constexpr int TILE_CH = 64;                      // staged candidates per chunk
-constexpr int TILE_BINS = 32;
-constexpr int TILE_OV = 16;                      // overflow keys per lane
-constexpr int TILE_OV_PITCH = TILE_OV + 1;       // u64 words per lane (odd: spreads banks)
+constexpr int TILE_BINS0 = 128;                  // level-0 bins (8-bit counts, four to a word)
+constexpr int TILE_BINS = 32;                    // bins of a refinement level (32-bit counts)
+constexpr int TILE_OV = 16;                      // overflow keys per query
 constexpr uint32_t TILE_MAX_ROWS = 4096;         // larger union boxes go to search_kernel
 
 struct alignas(16) Cand {
@@ -60,20 +64,32 @@ struct alignas(16) Cand {
   uint32_t id;
 };
 
+// Capacity of a query's key list: about twice k+1 (the learned radius
+// finds 1.4 (k+1) keys on average; the few queries that find more are
+// handed to search_kernel), the pitch in u64 words = 4 (mod 16) so that the
+// lists of the 8 queries of a warp spread over the banks.
+constexpr int tile_list_cap(int kmax) { return kmax >= 65 ? 132 : kmax >= 33 ? 84 : 52; }
+
 // shared memory of one warp (bytes): QPT queries with rows of up to KMAX
-// keys.  Pitches are odd (rows, overflow lists in u64 words; histograms in
-// u32 words), so queries at the same index fall in different banks.
+// keys.  The staging chunk, the refinement histograms and the rows' u16
+// list indices share one region (used one after another); a query's sorted
+// row is assembled at the start of its own list.
 template <int QPT, int KMAX>
 struct TileSmem {
-  static constexpr int KP = (KMAX % 2 == 1) ? KMAX : KMAX + 1;
-  static constexpr int HP = TILE_BINS + 1;
-  static constexpr int CAND = 0;
-  static constexpr int HIST = CAND + TILE_CH * 16;           // [QPT][HP] u32
-  static constexpr int AUX = HIST + QPT * HP * 4;             // [QPT][HP] u32 (refinement)
-  static constexpr int OVC = AUX + QPT * HP * 4;              // [QPT] u32 overflow counts
-  static constexpr int OV = (OVC + QPT * 4 + 7) / 8 * 8;      // [QPT][TILE_OV_PITCH] u64
-  static constexpr int ROWS = OV + QPT * TILE_OV_PITCH * 8;   // [QPT][KP] u64
-  static constexpr int RUNS = ROWS + QPT * KP * 8;            // 2 x 32 u32
+  static constexpr int C = tile_list_cap(KMAX);                 // list capacity per query (u64 keys)
+  static constexpr int HP = TILE_BINS + 1;                      // histogram pitch (u32 words)
+  static constexpr int RP = KMAX + 1;                           // row index pitch (u16)
+  static constexpr int SHARED_BYTES =
+      (TILE_CH * 16 > QPT * HP * 4 ? (TILE_CH * 16 > QPT * RP * 2 ? TILE_CH * 16 : QPT * RP * 2)
+                                   : (QPT * HP * 4 > QPT * RP * 2 ? QPT * HP * 4 : QPT * RP * 2));
+  static constexpr int LIST = 0;                                // [QPT][C] u64
+  static constexpr int CAND = LIST + QPT * C * 8;               // staging chunk | refinement bins | row indices
+  static constexpr int AUX = CAND;
+  static constexpr int RIDX = CAND;
+  static constexpr int HIST = (CAND + SHARED_BYTES + 15) / 16 * 16;  // [QPT][HP] u32
+  static constexpr int OVC = HIST + QPT * HP * 4;               // [QPT] u32 overflow counts
+  static constexpr int OVI = OVC + QPT * 4;                     // [QPT][TILE_OV] u16 overflow indices
+  static constexpr int RUNS = (OVI + QPT * TILE_OV * 2 + 15) / 16 * 16;  // 2 x 32 u32
   static constexpr int BYTES = RUNS + 2 * 32 * 4;
 };
 
@@ -104,12 +120,13 @@ struct TileParams {
   FailRadii* fail_radii;
 };
 
-// round(a * s + c) clamped to [0, 31], with the integer read from the low
-// mantissa bits of a + 1.5 * 2^23 (one FMA); monotone in a.  c must be an
-// integer (exact in float).
+// round(a * s + c) clamped to [0, NB - 1], with the integer read from the
+// low mantissa bits of a + 1.5 * 2^23 (one FMA); monotone in a.  c must be
+// an integer (exact in float).
+template <int NB>
 __device__ __forceinline__ int tbin(float a, float s, float cm) {
   const int v = __float_as_int(__fmaf_rn(a, s, cm)) - 0x4b400000;
-  return min(max(v, 0), TILE_BINS - 1);
+  return min(max(v, 0), NB - 1);
 }
 
 // Warp-aggregated append of this lane's value to a global list.
@@ -126,10 +143,11 @@ __device__ __forceinline__ void warp_append(bool want, uint32_t v, uint32_t* lis
 // QPT queries per warp (4, 8 or 16), LPQ = 32 / QPT lanes per query: lane
 // (slot qs = lane % QPT, phase ph = lane / QPT) evaluates the staged
 // candidates ph, ph + LPQ, ... for query qs.  The query's lanes share its
-// histogram, row and overflow list through shared-memory atomics; the lane
-// of phase 0 does the query's serial steps.
+// list, histogram, row indices and overflow list in shared memory; the lane
+// of phase 0 does the query's serial steps.  With 4 queries per warp the
+// kernel is held to 64 registers: 8 blocks of 4 warps fit an SM.
 template <int D, int KMAX, int QPT>
-__global__ void __launch_bounds__(TILE_THREADS, 5) tile_kernel(const TileParams p) {
+__global__ void __launch_bounds__(TILE_THREADS, QPT == 4 ? 8 : 5) tile_kernel(const TileParams p) {
   using SM = TileSmem<QPT, KMAX>;
   constexpr int LPQ = 32 / QPT;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -140,14 +158,21 @@ __global__ void __launch_bounds__(TILE_THREADS, 5) tile_kernel(const TileParams 
   const bool lead = ph == 0;
   unsigned char* ws = smem + (size_t)wib * SM::BYTES;
   Cand* cand = reinterpret_cast<Cand*>(ws + SM::CAND);
+  unsigned long long* lists = reinterpret_cast<unsigned long long*>(ws + SM::LIST);  // [QPT][C]
+  unsigned long long* mylist = lists + (size_t)qs * SM::C;  // this query's keys, later its row
   uint32_t* hq = reinterpret_cast<uint32_t*>(ws + SM::HIST) + qs * SM::HP;  // this query's bins
   uint32_t* aq = reinterpret_cast<uint32_t*>(ws + SM::AUX) + qs * SM::HP;
-  uint32_t* ovc = reinterpret_cast<uint32_t*>(ws + SM::OVC) + qs;
-  unsigned long long* myov = reinterpret_cast<unsigned long long*>(ws + SM::OV) + (size_t)qs * TILE_OV_PITCH;
-  unsigned long long* rows = reinterpret_cast<unsigned long long*>(ws + SM::ROWS);  // [QPT][KP]
-  unsigned long long* myrow = rows + (size_t)qs * SM::KP;
+  uint16_t* rowix = reinterpret_cast<uint16_t*>(ws + SM::RIDX);  // [QPT][RP] list indices by row slot
+  uint32_t* ovcs = reinterpret_cast<uint32_t*>(ws + SM::OVC);
+  uint32_t* ovc = ovcs + qs;
+  uint16_t* ovi = reinterpret_cast<uint16_t*>(ws + SM::OVI);  // [QPT][TILE_OV] list indices
   uint32_t* runS = reinterpret_cast<uint32_t*>(ws + SM::RUNS);
   uint32_t* runP = runS + 32;
+  // this query's lanes, and those of them below this lane
+  unsigned qmask = 0;
+#pragma unroll
+  for (int pp = 0; pp < LPQ; pp++) qmask |= 1u << (qs + QPT * pp);
+  const unsigned qbelow = qmask & lanemask_lt();
 
   __shared__ float s_minf[3];
   __shared__ float s_invw;
@@ -220,7 +245,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 5) tile_kernel(const TileParams 
     warp_append(defer && lead, qid, p.defer_list, p.defer_count, lane);
 
     const float thr = in ? within_threshold(r) : -1.0f;  // acc <= thr never holds off the tile
-    const float s0 = (thr > 0.0f && thr < 3.0e38f) ? __fdividef((float)TILE_BINS, thr) : 0.0f;
+    const float s0 = (thr > 0.0f && thr < 3.0e38f) ? __fdividef((float)TILE_BINS0, thr) : 0.0f;
     const float MAG = 12582912.0f;  // 1.5 * 2^23
 
     // Visits every candidate of the union box; body(c, live) runs on every
@@ -313,9 +338,68 @@ __global__ void __launch_bounds__(TILE_THREADS, 5) tile_kernel(const TileParams 
       }
       return acc;
     };
-    // zeroes a query's 32 bins (its LPQ lanes share the work)
+    // zeroes a query's 32 histogram words (its LPQ lanes share the work)
     auto clear_bins = [&](uint32_t* h) {
       for (int b = ph; b < TILE_BINS; b += LPQ) h[b] = 0u;
+    };
+
+    // The boundary search over one query's 128 level-0 bins, 8-bit counts
+    // packed four to a word (h[w] holds bins 4w .. 4w+3; every count and
+    // every prefix is at most the list capacity, below 256, so bytewise sums
+    // never carry): each of the query's LPQ lanes takes 32 / LPQ consecutive
+    // words, one multiply by 0x01010101 gives a word's inclusive prefix per
+    // byte, a scan over the query's lanes gives each lane its starting
+    // count, and the bins become their exclusive prefix.  Outputs as for
+    // walk_bins below; `multi` gets a bit for each of this lane's bins
+    // (32 / LPQ words from bin 128 / LPQ * ph on) holding two keys or more.
+    auto walk_bytes = [&](uint32_t* h, uint32_t& total, uint32_t& lo_cnt, uint32_t& mb, uint32_t& bstar,
+                          unsigned long long& multi) {
+      constexpr int WPL = 32 / LPQ;
+      uint32_t wv[WPL];
+      uint32_t part = 0;
+      multi = 0;
+#pragma unroll
+      for (int i = 0; i < WPL; i++) {
+        wv[i] = h[ph * WPL + i];
+        part += (wv[i] * 0x01010101u) >> 24;
+        // bytes of 2 or more (counts stay below 130: no carry), 4 bits per word
+        const uint32_t two = (wv[i] + 0x7e7e7e7eu) & 0x80808080u;
+        const uint32_t nib = ((two >> 7) & 1u) | ((two >> 14) & 2u) | ((two >> 21) & 4u) | ((two >> 28) & 8u);
+        multi |= (unsigned long long)nib << (4 * i);
+      }
+      uint32_t incl = part;
+#pragma unroll
+      for (int off = 1; off < LPQ; off <<= 1) {
+        const uint32_t tt = __shfl_up_sync(FULL, incl, off * QPT);
+        if (ph >= off) incl += tt;
+      }
+      uint32_t cum = incl - part;
+      uint32_t fb = TILE_BINS0, flo = 0, fm = 0;
+#pragma unroll
+      for (int i = 0; i < WPL; i++) {
+        const uint32_t w = wv[i];
+        const uint32_t pin = w * 0x01010101u;  // inclusive prefix within the word, per byte
+        h[ph * WPL + i] = (pin - w) + cum * 0x01010101u;
+        if (fb == TILE_BINS0 && cum + (pin >> 24) >= K) {
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            const uint32_t cj = (pin >> (8 * j)) & 0xffu;
+            if (fb == TILE_BINS0 && cum + cj >= K) {
+              fb = (uint32_t)(4 * (ph * WPL + i) + j);
+              fm = (w >> (8 * j)) & 0xffu;
+              flo = cum + cj - fm;
+            }
+          }
+        }
+        cum += pin >> 24;
+      }
+      total = __shfl_sync(FULL, incl, qs + QPT * (LPQ - 1));
+      const unsigned hit = __ballot_sync(FULL, fb != TILE_BINS0);
+      const unsigned mine = hit & qmask;
+      const int src = mine ? __ffs(mine) - 1 : qs;
+      bstar = __shfl_sync(FULL, fb, src);
+      lo_cnt = __shfl_sync(FULL, flo, src);
+      mb = __shfl_sync(FULL, fm, src);
     };
 
     // The boundary search over one query's 32 bins (counts h[b], base keys
@@ -353,9 +437,6 @@ __global__ void __launch_bounds__(TILE_THREADS, 5) tile_kernel(const TileParams 
       total = __shfl_sync(FULL, base + incl, qs + QPT * (LPQ - 1)) - base;
       // the first lane of the query (by phase) that found the boundary
       const unsigned hit = __ballot_sync(FULL, fb != TILE_BINS);
-      unsigned qmask = 0;
-#pragma unroll
-      for (int pp = 0; pp < LPQ; pp++) qmask |= 1u << (qs + QPT * pp);
       const unsigned mine = hit & qmask;
       const int src = mine ? __ffs(mine) - 1 : qs;
       bstar = __shfl_sync(FULL, fb, src);
@@ -363,52 +444,42 @@ __global__ void __launch_bounds__(TILE_THREADS, 5) tile_kernel(const TileParams 
       mb = __shfl_sync(FULL, fm, src);
     };
 
-    // 3. pass 1: counts per bin of squared distance within the radius
-    clear_bins(hq);
-    __syncwarp();
+    // 3. pass 1: every key within the radius is appended to the query's
+    // list (slots from a ballot over the query's lanes: no atomics); the
+    // count goes on past the capacity, so `found` is exact
+    uint32_t found = 0;
     const uint32_t box_points = for_each_candidate([&](const Cand& c, bool live) {
       const float acc = sqdist(c);
-      if (live && acc <= thr) atomicAdd(&hq[tbin(acc, s0, MAG)], 1u);
+      const bool want = live && acc <= thr;
+      const unsigned bal = __ballot_sync(FULL, want);
+      const uint32_t slot = found + (uint32_t)__popc(bal & qbelow);
+      if (want && slot < (uint32_t)SM::C)
+        mylist[slot] = ((unsigned long long)__float_as_uint(acc) << 32) | c.id;
+      found += (uint32_t)__popc(bal & qmask);
     });
     // candidates evaluated: the union box's points for every query it serves
     scanned += (unsigned long long)box_points * (unsigned)__popc(__ballot_sync(FULL, in && lead));
+    // a query with more keys than its list holds goes to search_kernel
+    const bool big = in && found > (uint32_t)SM::C;
+    warp_append(big && lead, qid, p.defer_list, p.defer_count, lane);
+    bool ok = in && found >= K && !big;
+    const uint32_t nl = ok ? found : 0u;  // list entries of an accepted query
     __syncwarp();
-    // boundary bin of level 0 and the counts below it; the query's LPQ lanes
-    // each take 32 / LPQ consecutive bins, and its bins become the exclusive
-    // prefix
-    uint32_t found = 0, c_lo = 0, m = 0, bs0 = TILE_BINS;
-    walk_bins(hq, 0u, true, found, c_lo, m, bs0);
-    bool ok = in && found >= K;
-    // Only keys in bins up to the boundary bin are wanted from here on: a
-    // key of bin <= bs0 has acc * s0 < bs0 + 1/2 (the bin is acc * s0
-    // rounded to nearest), so its point lies within radius
-    // sqrt((bs0 + 1/2) / s0), widened here by 2^-10; the refinement passes
-    // and pass 2 scan the union of the accepted queries' rings at that
-    // radius (the boundary bin sits near the middle of the radius' range of
-    // squared distances, so the box is about half as large).
-    {
-      float rp = 0.0f;
-      if (ok && bs0 < (uint32_t)TILE_BINS - 1 && s0 > 0.0f)
-        rp = fminf(sqrtf(((float)bs0 + 0.5f) / s0 * (1.0f + 1.0f / 1048576.0f)) * (1.0f + 1.0f / 1024.0f), r);
-      else if (ok)
-        rp = r;
-      const float rpf = rp * (1.0f + 1.0f / 8192.0f);
-#pragma unroll
-      for (int j = 0; j < D; j++) {
-        const float slack = (fabsf(q[j]) + rpf) * (1.0f / 2097152.0f);
-        const uint32_t l2 = ring_cell(q[j] - rpf - slack, s_minf[j], s_invw, p.g.ncell[j], false);
-        const uint32_t h2 = ring_cell(q[j] + rpf + slack, s_minf[j], s_invw, p.g.ncell[j], true);
-        LO[j] = __reduce_min_sync(FULL, ok ? l2 : 0xffffffffu);
-        HI[j] = __reduce_max_sync(FULL, ok ? h2 : 0u);
-      }
-      if (__any_sync(FULL, ok)) {
-        ext1 = HI[1] - LO[1] + 1;
-        ext2 = D == 3 ? HI[D - 1] - LO[D - 1] + 1 : 1u;
-        nrows = ext1 * ext2;  // (within the first box: at most TILE_MAX_ROWS)
-      } else {
-        nrows = 0;
-      }
+
+    // 128 bins of squared distance over the list (8-bit counts), the
+    // boundary bin of level 0 and the counts below it; the bins become their
+    // exclusive prefix
+    clear_bins(hq);
+    __syncwarp();
+    for (uint32_t e = (uint32_t)ph; e < nl; e += LPQ) {
+      const int b = tbin<TILE_BINS0>(__uint_as_float((uint32_t)(mylist[e] >> 32)), s0, MAG);
+      atomicAdd(&hq[b >> 2], 1u << (8 * (b & 3)));
     }
+    __syncwarp();
+    uint32_t listed = 0, c_lo = 0, m = 0, bs0 = TILE_BINS0;
+    unsigned long long multi = 0;
+    walk_bytes(hq, listed, c_lo, m, bs0, multi);
+
     // refinement of the boundary bin while it overflows the overflow list
     int lev = 0;
     int bs[3] = {(int)bs0, TILE_BINS, TILE_BINS};
@@ -423,16 +494,17 @@ __global__ void __launch_bounds__(TILE_THREADS, 5) tile_kernel(const TileParams 
         clear_bins(aq);
       }
       __syncwarp();
-      for_each_candidate([&](const Cand& c, bool live) {
-        const float acc = sqdist(c);
-        if (live && need && acc <= thr && tbin(acc, sl[0], MAG) == bs[0]) {
+      if (need) {
+        for (uint32_t e = (uint32_t)ph; e < nl; e += LPQ) {
+          const float acc = __uint_as_float((uint32_t)(mylist[e] >> 32));
+          if (tbin<TILE_BINS0>(acc, sl[0], MAG) != bs[0]) continue;
           bool member = true;
 #pragma unroll
           for (int l2 = 1; l2 < L; l2++)
-            if (tbin(acc, sl[l2], MAG + cl[l2]) != bs[l2]) member = false;
-          if (member) atomicAdd(&aq[tbin(acc, sl[L], MAG + cl[L])], 1u);
+            if (tbin<TILE_BINS>(acc, sl[l2], MAG + cl[l2]) != bs[l2]) member = false;
+          if (member) atomicAdd(&aq[tbin<TILE_BINS>(acc, sl[L], MAG + cl[L])], 1u);
         }
-      });
+      }
       __syncwarp();
       uint32_t nb = TILE_BINS, nlo = c_lo, nm = m, ntot = 0;
       walk_bins(aq, c_lo, false, ntot, nlo, nm, nb);
@@ -450,86 +522,111 @@ __global__ void __launch_bounds__(TILE_THREADS, 5) tile_kernel(const TileParams 
     warp_append(tie_defer && lead, qid, p.defer_list, p.defer_count, lane);
     ok = ok && !tie_defer;
 
-    // 4. pass 2: keys below the boundary bin to their bin's running slot,
+    // 4. placement: the list index of every key below the boundary bin goes
+    // to its bin's running slot of the row (a counting sort by bin), the
     // keys of the boundary bin to the overflow list
     if (lead) *ovc = 0u;
     __syncwarp();
-    if (__any_sync(FULL, ok)) {
-      for_each_candidate([&](const Cand& c, bool live) {
-        const float acc = sqdist(c);
-        if (live && ok && acc <= thr) {
-          const int b0 = tbin(acc, sl[0], MAG);
-          bool place = b0 < bs[0];
-          bool over = b0 == bs[0] && lev == 0;
-          if (b0 == bs[0] && lev > 0) {  // (refined boundary bins only)
-            const int b1 = tbin(acc, sl[1], MAG + cl[1]);
-            if (b1 < bs[1]) {
-              place = true;
-            } else if (b1 == bs[1]) {
-              if (lev == 1) {
-                over = true;
-              } else {
-                const int b2 = tbin(acc, sl[2], MAG + cl[2]);
-                place = b2 < bs[2];
-                over = b2 == bs[2];
-              }
+    if (ok) {
+      uint16_t* myridx = rowix + qs * SM::RP;
+      uint16_t* myovi = ovi + qs * TILE_OV;
+      for (uint32_t e = (uint32_t)ph; e < nl; e += LPQ) {
+        const float acc = __uint_as_float((uint32_t)(mylist[e] >> 32));
+        const int b0 = tbin<TILE_BINS0>(acc, sl[0], MAG);
+        bool place = b0 < bs[0];
+        bool over = b0 == bs[0] && lev == 0;
+        if (b0 == bs[0] && lev > 0) {  // (refined boundary bins only)
+          const int b1 = tbin<TILE_BINS>(acc, sl[1], MAG + cl[1]);
+          if (b1 < bs[1]) {
+            place = true;
+          } else if (b1 == bs[1]) {
+            if (lev == 1) {
+              over = true;
+            } else {
+              const int b2 = tbin<TILE_BINS>(acc, sl[2], MAG + cl[2]);
+              place = b2 < bs[2];
+              over = b2 == bs[2];
             }
           }
-          const unsigned long long key = ((unsigned long long)__float_as_uint(acc) << 32) | c.id;
-          if (place) myrow[atomicAdd(&hq[b0], 1u)] = key;
-          if (over) myov[atomicAdd(ovc, 1u)] = key;
         }
-      });
+        if (place) {
+          const int sh = 8 * (b0 & 3);
+          myridx[(atomicAdd(&hq[b0 >> 2], 1u << sh) >> sh) & 0xffu] = (uint16_t)e;
+        }
+        if (over) myovi[atomicAdd(ovc, 1u)] = (uint16_t)e;
+      }
     }
     __syncwarp();
 
-    // 5. rows in order: after pass 2, bin b < bs0 holds slots [hq[b-1], hq[b])
-    // and the placed part of the boundary bin [hq[bs0-1], hq[bs0]); the
-    // query's lanes insertion-sort these short ranges (keys of one bin) in
-    // parallel, one lane also sorts the overflow list, and the smallest
-    // overflow keys complete the row
-    const uint32_t nov = *ovc;
-    auto isort = [](unsigned long long* a, uint32_t lo, uint32_t hi) {
+    // 5. rows in order: after placement the byte of bin b <= bs0 holds the
+    // end of its slots (its start is the end of bin b - 1); only the bins
+    // the histogram found with two keys or more need ordering (the bins are
+    // narrow: 0.7 keys on average), and one lane sorts the overflow indices,
+    // whose smallest complete the row
+    auto isort_idx = [&](uint16_t* a, uint32_t lo, uint32_t hi) {
       for (uint32_t i = lo + 1; i < hi; i++) {
-        const unsigned long long key = a[i];
+        const uint16_t ix = a[i];
+        const unsigned long long key = mylist[ix];
         uint32_t j = i;
         while (j > lo) {
-          const unsigned long long prev = a[j - 1];
-          if (prev <= key) break;
-          a[j] = prev;
+          const uint16_t pix = a[j - 1];
+          if (mylist[pix] <= key) break;
+          a[j] = pix;
           j--;
         }
-        a[j] = key;
+        a[j] = ix;
+      }
+    };
+    auto sort_idx = [&](uint16_t* a, uint32_t lo, uint32_t hi) {
+      if (hi - lo == 2) {
+        const uint16_t i0 = a[lo], i1 = a[lo + 1];
+        if (mylist[i1] < mylist[i0]) {
+          a[lo] = i1;
+          a[lo + 1] = i0;
+        }
+      } else if (hi - lo > 2) {
+        isort_idx(a, lo, hi);
       }
     };
     if (ok) {
-      constexpr int BPL = TILE_BINS / LPQ;
-#pragma unroll 1
-      for (int i = 0; i < BPL; i++) {
-        const int b = ph * BPL + i;
-        if (b > bs[0]) break;
-        const uint32_t lo_s = b == 0 ? 0u : hq[b - 1];
-        const uint32_t hi_s = hq[b];
-        if (hi_s - lo_s > 1) isort(myrow, lo_s, hi_s);
+      constexpr int BPL = TILE_BINS0 / LPQ;  // bins per lane
+      uint16_t* myridx = rowix + qs * SM::RP;
+      // this lane's bins with placed keys: up to bs0 (bs0 itself only when
+      // refined: otherwise its keys are in the overflow list)
+      const int top = bs[0] - (lev == 0 ? 1 : 0) - BPL * ph;
+      unsigned long long mm = top < 0 ? 0ull : (top >= BPL - 1 ? multi : multi & ((2ull << top) - 1ull));
+      // a refined boundary bin is sorted whatever its count (a count above
+      // 129 would not show in the bytewise test)
+      if (lev > 0 && top >= 0 && top < BPL) mm |= 1ull << top;
+      while (mm) {
+        const int b = BPL * ph + __ffsll((long long)mm) - 1;
+        mm &= mm - 1;
+        const uint32_t w = hq[b >> 2];
+        const int j = b & 3;
+        const uint32_t hi = (w >> (8 * j)) & 0xffu;
+        const uint32_t lo = j ? (w >> (8 * (j - 1))) & 0xffu : (b ? hq[(b >> 2) - 1] >> 24 : 0u);
+        sort_idx(myridx, lo, hi);
       }
-      if (ph == LPQ - 1) isort(myov, 0u, nov);
+      if (ph == LPQ - 1) sort_idx(ovi + qs * TILE_OV, 0u, *ovc);
     }
     __syncwarp();
-    if (ok)
-      for (uint32_t i = c_lo + (uint32_t)ph; i < K; i += LPQ) myrow[i] = myov[i - c_lo];
-    __syncwarp();
-    // coalesced row writes: the warp writes each accepted query's row
+    // coalesced row writes: the warp writes each accepted query's row, slot
+    // s from the list entry of row index s (s < c_lo) or of overflow index
+    // s - c_lo
     {
       unsigned mask = __ballot_sync(FULL, ok && lead);
       while (mask) {
         const int rl = __ffs(mask) - 1;  // (a lead lane: its index is the query slot)
         mask &= mask - 1;
         const uint32_t rid = __shfl_sync(FULL, qid, rl);
-        const unsigned long long* src = rows + (size_t)rl * SM::KP;
+        const uint32_t rclo = __shfl_sync(FULL, c_lo, rl);
+        const unsigned long long* rlist = lists + (size_t)rl * SM::C;
+        const uint16_t* rix = rowix + rl * SM::RP;
+        const uint16_t* rov = ovi + rl * TILE_OV;
         const uint64_t base = (uint64_t)rid * K;
         float rsq = 0.0f;
         for (uint32_t s = (uint32_t)lane; s < K; s += 32) {
-          const unsigned long long key = src[s];
+          const unsigned long long key = rlist[s < rclo ? rix[s] : rov[s - rclo]];
           const float dist = __fsqrt_rn(__uint_as_float((uint32_t)(key >> 32)));
           p.out_ids[base + s] = (int32_t)(uint32_t)key;
           p.out_d[base + s] = dist;
@@ -617,9 +714,11 @@ void launch_tile_search(const SearchLaunch<T>& a, uint32_t* defer_list, uint32_t
     p.fail_radii = a.fail_radii;
     launch_zero_words(a.work_counter, sizeof(uint32_t), s);
     const bool d3 = a.d == 3;
-    // queries per tile: fewer queries per tile widen the union box less (a
-    // tile's queries cover a smaller share of one query's neighbourhood)
-    int qpt = 8;
+    // queries per tile: 8 share a box best (fewest candidates per query),
+    // but their lists need twice the shared memory of 4; with 4 (64
+    // registers, 8 blocks of 4 warps per SM) the kernel keeps 32 warps per
+    // SM against 20, and the tile kernel is bound by latency: 4 is faster
+    int qpt = 4;
     if (const char* e = std::getenv("KNNSJ_TILE_QPT")) qpt = std::atoi(e);
 #define KNNSJ_TILE_LAUNCH(QPT)                                                                 \
   do {                                                                                        \

@@ -33,15 +33,16 @@ struct JoinConfig {
   int search_buffer = 0;
   int tail_brute = 1;                      // a few queries whose radius outgrew the grid are finished by
                                            // an exact scan over all points (2: at any due rebuild; 0: off)
-  int row_chunks = 32;                     // host-pointer calls into pinned buffers: rows streamed out
+  int row_chunks = 32;                     // with direct_rows 0: rows streamed out of the device table
                                            // in this many blocks while the join runs (< 2: at the end)
   int tile_search = 1;                     // first pass of 2-D / 3-D float data over a finer grid: 0 off,
                                            // 1 query tiles (k_tile.cu) for per-query radii and one warp
                                            // per query for a uniform radius, 2 always one warp per query,
                                            // 3 always query tiles
   int tile_fine = 0;                       // that grid's cells: eps0 / tile_fine (0: 4 for tiles, 2 else)
-  int direct_rows = 1;                     // pinned outputs take their rows straight from the kernels
-                                           // (0: streamed from a device table by the copy engines)
+  int direct_rows = 2;                     // pinned outputs: 2 a device table copied into them by an SM
+                                           // kernel after the join, 1 rows straight from the search
+                                           // kernels, 0 a device table streamed by the copy engines
   unsigned long long device_table_cap = 0; // largest device result table (bytes) before pageable outputs
                                            // are registered and written directly; 0 = free memory less 2 GB
 };

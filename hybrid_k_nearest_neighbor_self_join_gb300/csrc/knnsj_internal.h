@@ -231,6 +231,7 @@ void launch_tile_search(const SearchLaunch<T>& a, uint32_t* defer_list, uint32_t
 // Clears bytes (a multiple of 4) with a kernel: unlike a runtime memset it
 // never waits behind copies in flight on another stream.
 void launch_zero_words(void* p, size_t bytes, cudaStream_t s);
+void launch_copy_to_mapped(void* dst, const void* src, size_t bytes, int sm_count, cudaStream_t s);
 int search_buffer_capacity(uint32_t K);
 // Exact rows of the queries a.qlist[0..a.nq) by a scan over all points.
 template <typename T>

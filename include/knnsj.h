@@ -158,16 +158,18 @@ void KNNJoinPy(float* dataset, unsigned int NUMPOINTS, unsigned int kNN, unsigne
 /* Status-returning self-join on HOST buffers (same pipeline as KNNJoinPy,
  * dtype chosen per call).  data: row-major n x d; outputs as above.  When
  * both outputs are pinned and mapped (cudaHostAlloc, or cudaHostRegister
- * with cudaHostRegisterMapped), the search kernels write every row straight
- * into them while the join runs: no device result table, no copy after the
- * join (KNNSJ_DIRECT_ROWS=0 instead copies rows out of a device table in
- * KNNSJ_ROW_CHUNKS blocks of query ids while the join runs).  Pageable
- * outputs get a device result table copied out after the join; when that
- * table would not fit in device memory (or exceeds opts->device_table_mb),
- * they are registered with the device for the call and written directly
- * instead (the memory-bounded mode).  The call returns when every row is in
- * place, also on error (no kernel or copy is left writing into the outputs).
- * stats may be NULL. */
+ * with cudaHostRegisterMapped), a kernel copies the device result table into
+ * them through their mapped addresses after the join (KNNSJ_DIRECT_ROWS=1
+ * instead has the search kernels write every row straight into them, with
+ * no device result table; KNNSJ_DIRECT_ROWS=0 streams rows out of a device
+ * table by the copy engines in KNNSJ_ROW_CHUNKS blocks of query ids while
+ * the join runs).  Pageable outputs get a device result table copied out
+ * after the join.  When the table would not fit in device memory (or
+ * exceeds opts->device_table_mb), the outputs (pageable ones registered with
+ * the device for the call) take their rows straight from the kernels: the
+ * memory-bounded mode.  The call returns when every row is in place, also
+ * on error (no kernel or copy is left writing into the outputs).  stats may
+ * be NULL. */
 knnsj_status knnsj_selfjoin(const void* data, knnsj_dtype dtype, uint64_t n, uint32_t d,
                             uint32_t k, const knnsj_options* opts, int32_t* out_ids,
                             void* out_dists, knnsj_stats* stats);

@@ -53,10 +53,11 @@ def test_iteration_cap_reports_no_convergence(monkeypatch, graph):
     assert np.array_equal(dists.view(np.uint32), odists.view(np.uint32))
 
 
-@pytest.mark.parametrize("direct", ["1", "0"])
+@pytest.mark.parametrize("direct", ["2", "1", "0"])
 def test_iteration_cap_with_pinned_outputs_leaves_nothing_in_flight(monkeypatch, direct):
-    # direct "1": rows written by the kernels into the pinned buffers;
-    # "0": rows streamed out of a device table by copies
+    # direct "2": a device table copied in by a kernel after the join; "1":
+    # rows written by the kernels into the pinned buffers; "0": rows streamed
+    # out of a device table by copies
     monkeypatch.setenv("KNNSJ_DIRECT_ROWS", direct)
     torch = pytest.importorskip("torch")
     n, k = 300_000, 8  # >= 2^18 rows: with direct "0" the rows are streamed during the join

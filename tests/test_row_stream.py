@@ -1,7 +1,9 @@
 """Where the rows of host-pointer joins go, and that they are the same rows.
 
-* pinned output buffers (default): the search kernels write every row
-  straight into them (no device result table, no copy);
+* pinned output buffers (default): a kernel copies the device result table
+  into them through their mapped addresses after the join;
+* pinned buffers with KNNSJ_DIRECT_ROWS=1: the search kernels write every
+  row straight into them (no device result table, no copy);
 * pinned buffers with KNNSJ_DIRECT_ROWS=0: rows in blocks of query ids
   copied out while the join runs, later passes' rows patched in at the end;
 * pageable buffers whose result table is larger than the device-table cap
@@ -55,6 +57,38 @@ def same(ids, dd, ref_i, ref_d):
     assert np.array_equal(ids, ref_i)
     bits = np.uint32 if dd.dtype == np.float32 else np.uint64
     assert np.array_equal(dd.view(bits), ref_d.view(bits))
+
+
+@pytest.mark.parametrize("mode,dtype", [(kj.RADIUS_LEARNED, np.float32), (kj.RADIUS_PLAIN, np.float32),
+                                        (kj.RADIUS_LEARNED, np.float64)])
+def test_table_copied_into_pinned_buffers(monkeypatch, mode, dtype):
+    n, k = 400_000, 32
+    x = datasets.sky_like(n, seed=37).astype(dtype)
+    ref_i, ref_d, ref_sum = reference(x, k, mode, monkeypatch)
+    monkeypatch.delenv("KNNSJ_DIRECT_ROWS", raising=False)
+    t_i, ids = pinned((n, k + 1), np.int32)
+    t_d, dd = pinned((n, k + 1), dtype)
+    ids[:] = -7
+    dd[:] = np.nan
+    _, _, st = kj.selfjoin(x, k, beta=0.025, radius_mode=mode, out_ids=ids, out_dists=dd, return_stats=True)
+    same(ids, dd, ref_i, ref_d)
+    close_sum(st["total_distance"], ref_sum)
+    # an odd-sized table (its byte count not a multiple of 16) into buffers
+    # offset by 4 bytes: the copy falls back to 4-byte words
+    m = 100_003
+    y = np.ascontiguousarray(x[:m])
+    yi, yd = kj.selfjoin(y, 6, beta=0.025, radius_mode=mode)
+    t_i2, ids2 = pinned((m * 7 + 1,), np.int32)
+    t_d2, dd2 = pinned((m * 7 + 1,), dtype)
+    oi = ids2[1:].reshape(m, 7)
+    od = dd2[1:].reshape(m, 7)
+    kj.selfjoin(y, 6, beta=0.025, radius_mode=mode, out_ids=oi, out_dists=od)
+    same(oi, od, yi, yd)
+    # aligned buffers of that odd size: 16-byte copies and a 4-byte tail
+    t_i3, ids3 = pinned((m, 7), np.int32)
+    t_d3, dd3 = pinned((m, 7), dtype)
+    kj.selfjoin(y, 6, beta=0.025, radius_mode=mode, out_ids=ids3, out_dists=dd3)
+    same(ids3, dd3, yi, yd)
 
 
 @pytest.mark.parametrize("mode,dtype,graph", [(kj.RADIUS_LEARNED, np.float32, "1"),
