@@ -384,7 +384,7 @@ def run_gb300(args):
     fp32_ach = fl / (kms / 1e3) / 1e12
     roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"], "traffic": tr["dram_bytes_per_join"] if tr else None,
-                "kernel": ("search kernels: tile_kernel<2,65,8> (first pass, query tiles) + search_kernel<float,2,2> "
+                "kernel": ("search kernels: tile_kernel<2,65,4> (first pass, query tiles) + search_kernel<float,2,2> "
                            "(retries and hand-overs)"), "kernel_ms_per_step": kms, "launches_per_step":
                 st["iterations"], "alg_bytes_per_step": ab,
                 "peak_source": f"{pk['source']} hbm_gbs (MEASURED_PEAKS.json): frac is of {pk['source']}",
