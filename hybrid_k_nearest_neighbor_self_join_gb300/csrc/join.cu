@@ -475,15 +475,16 @@ __global__ void defer_roll_kernel(uint32_t* __restrict__ count, unsigned long lo
 }  // namespace
 
 // Set-up of the tile search for the first pass: the order in which tiles
-// take the queries (Morton order of their cells on a grid 16 times finer
-// than eps0, so that consecutive queries are close in every dimension) and
+// take the queries (Hilbert or Morton order of their cells on a grid 16
+// times finer than eps0, so that consecutive queries are close in every
+// dimension) and
 // the grid the candidates come from (a finer grid of width eps0 / f when its
 // dense table fits).
 template <typename T>
 struct TileSetup {
   bool on = false;
   DeviceGrid<T> cand;                 // candidate grid
-  const uint32_t* qorder = nullptr;   // positions of the eps0 grid's cell order, in tile order (Morton)
+  const uint32_t* qorder = nullptr;   // positions of the eps0 grid's cell order, in tile order
   int fine = 1;                       // eps0 / candidate cell width
   bool per_query = false;             // search_kernel (one warp per query) on the candidate grid
 };
@@ -497,16 +498,17 @@ static void prepare_tile(Workspace& w, bool tiles, int fine_max, const DeviceGri
   sc.scan_tmp_elems = scan_tmp_elems(std::max<size_t>(sc.hist_elems, n + 1));
   t->per_query = !tiles;
   if (tiles) {
-  // 1. Morton order of the points' cells on a grid 16 times finer than eps0
+  // 1. order of the points' cells along a space-filling curve (Hilbert in
+  // two dimensions, Morton otherwise) on a grid 16 times finer than eps0
   // (stable: cell order within a cell), so that the few queries of a tile
   // lie close together, not anywhere in one eps0 cell: the union box of
   // their rings then stays near the size of one ring
-  constexpr int MORTON_FINE = 16;
+  constexpr int ORDER_FINE = 16;
   GridGeom<T> gm = g.geom;
-  gm.width = (T)((double)eps0 / MORTON_FINE);
+  gm.width = (T)((double)eps0 / ORDER_FINE);
   int bits = 1;
   for (uint32_t j = 0; j < di; j++)
-    while (bits < 21 && (1ull << bits) < (unsigned long long)g.geom.ncell[j] * MORTON_FINE) bits++;
+    while (bits < 21 && (1ull << bits) < (unsigned long long)g.geom.ncell[j] * ORDER_FINE) bits++;
   sc.keys[0] = (unsigned long long*)w.keys0.get(n * 8);
   sc.keys[1] = (unsigned long long*)w.keys1.get(n * 8);
   sc.vals[0] = (uint32_t*)w.vals0.get(n * 4);

@@ -275,17 +275,41 @@ __global__ void gather_sorted_kernel(const T* __restrict__ soa, uint64_t n, uint
   }
 }
 
-// Morton (Z-order) code of a point's cell over the di indexed dimensions,
-// `bits` bits per dimension: bit b of cell coordinate j goes to bit b*di + j.
+// Position of a point's cell along a space-filling curve over the di indexed
+// dimensions, `bits` bits per dimension (a code of bits * di bits).  Two
+// dimensions: the Hilbert curve (the published xy-to-d conversion: per level
+// from the top, the quadrant's index (3 rx) ^ ry, then the quadrant is
+// rotated or flipped into the curve's frame), whose consecutive cells are
+// always adjacent; otherwise the Morton (Z-order) code, bit b of cell
+// coordinate j at bit b*di + j.
 template <typename T>
 __global__ void morton_key_kernel(const T* __restrict__ ps, uint64_t n, const GridGeom<T> g, int bits,
                                   unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
     unsigned long long code = 0;
-    for (uint32_t j = 0; j < g.di; j++) {
-      const uint32_t c = point_cell_coord(ps[(uint64_t)j * n + i], g.minv[j], g.width);
-      for (int b = 0; b < bits; b++) code |= (unsigned long long)((c >> b) & 1u) << (b * g.di + j);
+    if (g.di == 2) {
+      const unsigned long long side = 1ull << bits;  // cell coordinates are below it
+      unsigned long long x = point_cell_coord(ps[i], g.minv[0], g.width);
+      unsigned long long y = point_cell_coord(ps[n + i], g.minv[1], g.width);
+      for (unsigned long long h = side >> 1; h > 0; h >>= 1) {
+        const unsigned long long rx = (x & h) ? 1ull : 0ull, ry = (y & h) ? 1ull : 0ull;
+        code += h * h * ((3ull * rx) ^ ry);
+        if (ry == 0) {
+          if (rx == 1) {
+            x = side - 1 - x;
+            y = side - 1 - y;
+          }
+          const unsigned long long t = x;
+          x = y;
+          y = t;
+        }
+      }
+    } else {
+      for (uint32_t j = 0; j < g.di; j++) {
+        const uint32_t c = point_cell_coord(ps[(uint64_t)j * n + i], g.minv[j], g.width);
+        for (int b = 0; b < bits; b++) code |= (unsigned long long)((c >> b) & 1u) << (b * g.di + j);
+      }
     }
     keys[i] = code;
     vals[i] = (uint32_t)i;
