@@ -64,11 +64,13 @@ struct alignas(16) Cand {
   uint32_t id;
 };
 
-// Capacity of a query's key list: about twice k+1 (the learned radius
+// Capacity of a query's key list: more than twice k+1 (the learned radius
 // finds 1.4 (k+1) keys on average; the few queries that find more are
-// handed to search_kernel), the pitch in u64 words = 4 (mod 16) so that the
-// lists of the 8 queries of a warp spread over the banks.
-constexpr int tile_list_cap(int kmax) { return kmax >= 65 ? 132 : kmax >= 33 ? 84 : 52; }
+// handed to search_kernel: 1.1 % of the sky join with 132 entries for
+// k+1 = 65, about 0.2 % with 148, the most that 8 blocks of 4 warps of 4
+// queries leave room for), the pitch in u64 words = 4 (mod 16) so that the
+// lists of a warp's queries spread over the banks.
+constexpr int tile_list_cap(int kmax) { return kmax >= 65 ? 148 : kmax >= 33 ? 84 : 52; }
 
 // shared memory of one warp (bytes): QPT queries with rows of up to KMAX
 // keys.  The staging chunk, the refinement histograms and the rows' u16
@@ -362,7 +364,9 @@ __global__ void __launch_bounds__(TILE_THREADS, QPT == 4 ? 8 : 5) tile_kernel(co
       for (int i = 0; i < WPL; i++) {
         wv[i] = h[ph * WPL + i];
         part += (wv[i] * 0x01010101u) >> 24;
-        // bytes of 2 or more (counts stay below 130: no carry), 4 bits per word
+        // bytes of 2 or more, 4 bits per word (a byte's carry only reaches
+        // bins above one of 130 keys or more, which lies at or above the
+        // boundary bin: the bins that get sorted hold fewer than K keys)
         const uint32_t two = (wv[i] + 0x7e7e7e7eu) & 0x80808080u;
         const uint32_t nib = ((two >> 7) & 1u) | ((two >> 14) & 2u) | ((two >> 21) & 4u) | ((two >> 28) & 8u);
         multi |= (unsigned long long)nib << (4 * i);
