@@ -204,7 +204,11 @@ def config_records(kj, torch, steps: int = 2) -> dict:
         tx = torch.from_numpy(x).cuda()
         tids = torch.empty((n, k + 1), dtype=torch.int32, device="cuda")
         td = torch.empty((n, k + 1), dtype=tx.dtype, device="cuda")
-        rec = {"n_points": n, "d": d, "k": k, "beta": beta, "num_indexed_dims": di, "dtype": str(x.dtype)}
+        # joins of a millisecond or so are timed over 20 calls, the large ones
+        # over `steps`
+        reps = steps if n > 1_000_000 else 20
+        rec = {"n_points": n, "d": d, "k": k, "beta": beta, "num_indexed_dims": di, "dtype": str(x.dtype),
+               "joins_timed": reps}
         tables = {}
         for label, mode in (("learned", kj.RADIUS_LEARNED), ("plain", kj.RADIUS_PLAIN)):
             kj.selfjoin_device(tx.data_ptr(), x.dtype, n, d, k, tids.data_ptr(), td.data_ptr(),
@@ -214,10 +218,10 @@ def config_records(kj, torch, steps: int = 2) -> dict:
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()
             sts = [kj.selfjoin_device(tx.data_ptr(), x.dtype, n, d, k, tids.data_ptr(), td.data_ptr(),
-                                      num_indexed_dims=di, beta=beta, radius_mode=mode) for _ in range(steps)]
+                                      num_indexed_dims=di, beta=beta, radius_mode=mode) for _ in range(reps)]
             e1.record()
             torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1) / steps
+            ms = e0.elapsed_time(e1) / reps
             st = sts[-1]
             r = {"ms_per_join": ms, "queries_per_s": n / (ms / 1e3), "iterations": st["iterations"],
                  "queries_run": st["queries_run"], "re_attempts": st["queries_run"] - n,
