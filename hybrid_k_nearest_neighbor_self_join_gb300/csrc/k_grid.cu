@@ -289,18 +289,20 @@ __global__ void morton_key_kernel(const T* __restrict__ ps, uint64_t n, const Gr
        i += (uint64_t)gridDim.x * blockDim.x) {
     unsigned long long code = 0;
     if (g.di == 2) {
-      const unsigned long long side = 1ull << bits;  // cell coordinates are below it
-      unsigned long long x = point_cell_coord(ps[i], g.minv[0], g.width);
-      unsigned long long y = point_cell_coord(ps[n + i], g.minv[1], g.width);
-      for (unsigned long long h = side >> 1; h > 0; h >>= 1) {
-        const unsigned long long rx = (x & h) ? 1ull : 0ull, ry = (y & h) ? 1ull : 0ull;
-        code += h * h * ((3ull * rx) ^ ry);
+      // (bits <= 21: coordinates and their flips stay in 32 bits; the
+      // quadrant indices enter the code two bits per level from the top)
+      const uint32_t last = (1u << bits) - 1u;  // cell coordinates are at most this
+      uint32_t x = point_cell_coord(ps[i], g.minv[0], g.width) & last;
+      uint32_t y = point_cell_coord(ps[n + i], g.minv[1], g.width) & last;
+      for (int l = bits - 1; l >= 0; l--) {
+        const uint32_t rx = (x >> l) & 1u, ry = (y >> l) & 1u;
+        code = (code << 2) | ((3u * rx) ^ ry);
         if (ry == 0) {
           if (rx == 1) {
-            x = side - 1 - x;
-            y = side - 1 - y;
+            x = last - x;
+            y = last - y;
           }
-          const unsigned long long t = x;
+          const uint32_t t = x;
           x = y;
           y = t;
         }
