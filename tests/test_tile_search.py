@@ -2,10 +2,10 @@
 the per-query search it replaces (KNNSJ_TILE=0), bit for bit.
 
 It covers both dimensions it serves (2-D and 3-D float, all indexed), the
-three row capacities (k+1 <= 16, 33, 65), the plain and learned starting
-radii, the streamed-rows path (its queries come by id blocks) and data whose
-boundary bin cannot be split (exact duplicates), which the tile hands over to
-the per-query search.
+three row capacities (k+1 <= 16, 33, 65), 4, 8 and 16 queries per warp, the
+plain and learned starting radii, the streamed-rows path (its queries come by
+id blocks) and data whose boundary bin cannot be split (exact duplicates),
+which the tile hands over to the per-query search.
 """
 import numpy as np
 import pytest
@@ -59,6 +59,18 @@ def test_tile_learned_equals_per_query_search(monkeypatch, d, k):
     same(a, c)
     same(a, e)
     same(a, f)
+
+
+@pytest.mark.parametrize("qpt", ["4", "8", "16"])
+@pytest.mark.parametrize("d,k", [(2, 64), (3, 16)])
+def test_tile_queries_per_warp(monkeypatch, qpt, d, k):
+    # 4 queries per warp is the default; 8 and 16 (KNNSJ_TILE_QPT) share a
+    # box among more queries with larger shared-memory lists
+    x = datasets.gmm(100_000, d, 20, 0.2, 17 + d + k, dtype=np.float32)
+    b, _ = join(x, k, 0.025, kj.RADIUS_LEARNED, False, monkeypatch)
+    monkeypatch.setenv("KNNSJ_TILE_QPT", qpt)
+    a, st = join(x, k, 0.025, kj.RADIUS_LEARNED, True, monkeypatch)
+    same(a, b)
 
 
 def test_tile_sky_like(monkeypatch):
