@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdio>
 #include <chrono>
 #include <cmath>
 #include <cstddef>
@@ -12,6 +13,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <vector>
@@ -389,6 +391,82 @@ std::vector<SearchShape> candidate_shapes(uint32_t K) {
   return v;
 }
 
+// Tuned shapes persist across processes in a text file named by
+// KNNSJ_TUNE_CACHE: one line per class, "<device> dtype d di K warps qchunk
+// buffer" (the device's name with blanks replaced by '_'); lines of other
+// devices are kept as they are.  The file is read the first time the batched
+// join runs on a device, and rewritten (through a temporary file and a
+// rename) whenever classes were tuned.  Only shapes the tuner itself would
+// try are taken from it.
+std::set<int> g_tune_loaded;   // devices whose cache file was read; guarded by g_call_mutex
+std::set<ShapeKey> g_measured;  // classes tuned by measurement here or in the file's process
+
+std::string device_tag(int dev) {
+  cudaDeviceProp p{};
+  if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return "unknown";
+  }
+  std::string t = p.name;
+  for (char& c : t)
+    if (c == ' ' || c == '\t') c = '_';
+  return t.empty() ? "unknown" : t;
+}
+
+bool tunable_shape(uint32_t K, const SearchShape& sh) {
+  if (sh.warps_per_block == 0 && sh.qchunk == 0 && sh.buffer == 0) return true;  // the default shape
+  for (const SearchShape& c : candidate_shapes(K))
+    if (c.warps_per_block == sh.warps_per_block && c.qchunk == sh.qchunk && c.buffer == sh.buffer) return true;
+  return false;
+}
+
+void load_tune_cache(int dev) {
+  const char* path = env("KNNSJ_TUNE_CACHE");
+  if (!path || !*path || g_tune_loaded.count(dev)) return;
+  g_tune_loaded.insert(dev);
+  FILE* f = std::fopen(path, "r");
+  if (!f) return;
+  const std::string tag = device_tag(dev);
+  char name[256];
+  int dt = 0;
+  unsigned d = 0, di = 0, K = 0;
+  SearchShape sh;
+  while (std::fscanf(f, "%255s %d %u %u %u %d %d %d", name, &dt, &d, &di, &K, &sh.warps_per_block, &sh.qchunk,
+                     &sh.buffer) == 8) {
+    if (tag == name && tunable_shape(K, sh)) {
+      g_tuned[ShapeKey{dt, d, di, K}] = sh;
+      g_measured.insert(ShapeKey{dt, d, di, K});
+    }
+  }
+  std::fclose(f);
+}
+
+void save_tune_cache(int dev) {
+  const char* path = env("KNNSJ_TUNE_CACHE");
+  if (!path || !*path) return;
+  const std::string tag = device_tag(dev);
+  std::string keep;  // other devices' lines
+  if (FILE* f = std::fopen(path, "r")) {
+    char line[512];
+    while (std::fgets(line, sizeof(line), f)) {
+      char name[256];
+      if (std::sscanf(line, "%255s", name) == 1 && tag != name) keep += line;
+    }
+    std::fclose(f);
+  }
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* f = std::fopen(tmp.c_str(), "w");
+  if (!f) return;
+  std::fputs(keep.c_str(), f);
+  for (const auto& kv : g_tuned)
+    if (g_measured.count(kv.first))
+      std::fprintf(f, "%s %d %u %u %u %d %d %d\n", tag.c_str(), kv.first.dtype, kv.first.d, kv.first.di, kv.first.K,
+                 kv.second.warps_per_block, kv.second.qchunk, kv.second.buffer);
+  const bool ok = std::fclose(f) == 0;
+  if (ok) std::rename(tmp.c_str(), path);
+  else std::remove(tmp.c_str());
+}
+
 struct BatchPool {
   std::vector<Workspace*> ws;  // one per worker, kept across calls
 };
@@ -430,6 +508,8 @@ void run_batched(knnsj_set* sets, const std::vector<uint32_t>& order, const std:
                     (T*)sets[i].out_dists, st, false);
   };
   // autotune the classes seen for the first time, on their largest set
+  load_tune_cache(dev);
+  bool tuned_now = false;
   const char* at = env("KNNSJ_AUTOTUNE");
   const bool tune = !(at && std::atoi(at) == 0);
   std::map<ShapeKey, uint32_t> largest;
@@ -456,12 +536,15 @@ void run_batched(knnsj_set* sets, const std::vector<uint32_t>& order, const std:
             best = sh;
           }
         }
+        g_measured.insert(kv.first);
+        tuned_now = true;
       } catch (...) {
         best = SearchShape();  // the set itself reports its error below
       }
     }
     g_tuned[kv.first] = best;
   }
+  if (tuned_now) save_tune_cache(dev);
   // run every set; workers take them largest first
   std::atomic<uint32_t> next{0};
   std::vector<knnsj_stats> per(order.size());

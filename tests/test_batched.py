@@ -63,3 +63,53 @@ def test_bad_set_reports_its_own_status():
     rc = lib.knnsj_selfjoin_batched(2, sets, _lib.KNNSJ_F32, ctypes.byref(opts), ctypes.byref(st))
     assert rc == 3 and sets[0].status == 3 and sets[1].status == 0  # KNNSJ_ERR_K_TOO_LARGE
     _check_same(outs[1:], [good], [8])
+
+
+_TUNE_SCRIPT = r"""
+import sys, json
+sys.path.insert(0, sys.argv[1])
+import numpy as np
+import hybrid_k_nearest_neighbor_self_join_gb300 as kj
+from hybrid_k_nearest_neighbor_self_join_gb300 import datasets
+xs = [datasets.gmm(30_000 + 1000 * i, 3, 6, 0.2, 40 + i, dtype=np.float32) for i in range(3)]
+outs = kj.selfjoin_batched(xs, [8, 8, 8])
+ok = all(np.array_equal(o[0], kj.selfjoin(x, 8)[0]) for o, x in zip(outs, xs))
+print(json.dumps({"ok": ok}))
+"""
+
+
+def test_tune_cache_persists_across_processes(tmp_path):
+    # KNNSJ_TUNE_CACHE: the first process tunes the class (float, d=3, k+1=9)
+    # and writes it; a second process loads it instead of tuning again (the
+    # shape planted in the file survives), and results stay those of single
+    # calls whatever the shape
+    import json
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cache = tmp_path / "tune.txt"
+    script = tmp_path / "tune_run.py"
+    script.write_text(_TUNE_SCRIPT)
+    env = dict(os.environ, KNNSJ_TUNE_CACHE=str(cache))
+    env.pop("KNNSJ_AUTOTUNE", None)
+
+    def run():
+        r = subprocess.run([sys.executable, str(script), root], env=env, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        assert json.loads(r.stdout.strip().splitlines()[-1])["ok"]
+
+    run()
+    lines = [ln.split() for ln in cache.read_text().splitlines() if ln.strip()]
+    mine = [ln for ln in lines if ln[1:5] == ["0", "3", "3", "9"]]
+    assert len(mine) == 1, lines
+    # plant another shape the tuner tries (4 warps per block, one query per
+    # fetch) and a line of another device, then run again
+    mine[0][5:8] = ["4", "1", "0"]
+    planted = " ".join(mine[0])
+    other = "Some_Other_GPU 0 3 3 9 8 16 0"
+    cache.write_text(planted + "\n" + other + "\n")
+    run()
+    # no class was tuned in the second process: the file is as planted
+    assert cache.read_text() == planted + "\n" + other + "\n"
