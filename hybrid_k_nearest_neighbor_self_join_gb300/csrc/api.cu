@@ -95,8 +95,19 @@ knnsj_status validate(const void* data, uint64_t n, uint32_t d, uint32_t k, cons
   if (n == 0 || d == 0 || d > (uint32_t)MAX_D) return KNNSJ_ERR_INVALID_ARGUMENT;
   if (n >= (1ull << 31)) return KNNSJ_ERR_TOO_MANY_POINTS;
   if ((uint64_t)k + 1 > n) return KNNSJ_ERR_K_TOO_LARGE;
-  if (k + 1 > 2048) return KNNSJ_ERR_UNSUPPORTED;
   return KNNSJ_OK;
+}
+
+// Largest k+1 of a join.  The search kernels keep each query's selection in
+// a shared-memory buffer of the next power of two >= k+1 + 32 keys (8-byte
+// keys for float data, 16-byte for double); one warp per block holds up to
+// 128 KB of it: k+1 up to 16352 (float) or 8160 (double).  The reference
+// has no such limit (its rows come from pair buffers on the host).
+constexpr uint32_t MAX_K_F32 = (128u << 10) / 8 - 32;
+constexpr uint32_t MAX_K_F64 = (128u << 10) / 16 - 32;
+
+knnsj_status k_supported(uint32_t k, knnsj_dtype dt) {
+  return (uint64_t)k + 1 <= (dt == KNNSJ_F64 ? MAX_K_F64 : MAX_K_F32) ? KNNSJ_OK : KNNSJ_ERR_UNSUPPORTED;
 }
 
 int select_device(const knnsj_options* o) {
@@ -669,6 +680,8 @@ knnsj_status knnsj_selfjoin(const void* data, knnsj_dtype dtype, uint64_t n, uin
   knnsj_status v = validate(data, n, d, k, out_ids, out_dists);
   if (v != KNNSJ_OK) return v;
   if (dtype != KNNSJ_F32 && dtype != KNNSJ_F64) return KNNSJ_ERR_INVALID_ARGUMENT;
+  v = k_supported(k, dtype);
+  if (v != KNNSJ_OK) return v;
   JoinConfig cfg;
   v = make_config(opts, d, &cfg);
   if (v != KNNSJ_OK) return v;
@@ -691,6 +704,8 @@ knnsj_status knnsj_selfjoin_device(const void* d_data, knnsj_dtype dtype, uint64
   knnsj_status v = validate(d_data, n, d, k, d_out_ids, d_out_dists);
   if (v != KNNSJ_OK) return v;
   if (dtype != KNNSJ_F32 && dtype != KNNSJ_F64) return KNNSJ_ERR_INVALID_ARGUMENT;
+  v = k_supported(k, dtype);
+  if (v != KNNSJ_OK) return v;
   JoinConfig cfg;
   v = make_config(opts, d, &cfg);
   if (v != KNNSJ_OK) return v;
@@ -749,6 +764,7 @@ knnsj_status knnsj_selfjoin_batched(uint32_t n_sets, knnsj_set* sets, knnsj_dtyp
   for (uint32_t i = 0; i < n_sets; i++) {
     knnsj_set& st = sets[i];
     st.status = validate(st.data, st.n, st.d, st.k, st.out_ids, st.out_dists);
+    if (st.status == KNNSJ_OK) st.status = k_supported(st.k, dtype);
     if (st.status == KNNSJ_OK) st.status = make_config(opts, st.d, &cfgs[i]);
     order.push_back(i);
   }

@@ -46,7 +46,7 @@ typedef enum {
   KNNSJ_ERR_CUDA = 7,             /* CUDA runtime error */
   KNNSJ_ERR_OUT_OF_MEMORY = 8,
   KNNSJ_ERR_NO_DEVICE = 9,
-  KNNSJ_ERR_UNSUPPORTED = 10,     /* e.g. NUMINDEXEDDIM > 8, k+1 > 2048 */
+  KNNSJ_ERR_UNSUPPORTED = 10,     /* e.g. NUMINDEXEDDIM > 8, k+1 > 16352 (float) or 8160 (double) */
   KNNSJ_ERR_IO = 11,              /* file could not be read or written */
   KNNSJ_ERR_EXCEEDS_FIXED_SCRATCH = 12 /* knnsj_selfjoin_device_noalloc: problem too large */
 } knnsj_status;

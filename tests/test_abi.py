@@ -125,6 +125,28 @@ def test_argument_errors_without_device():
     assert _call(x, 100, 2, 4, dtype=7) == 1
 
 
+def test_k_cap_by_dtype_without_device():
+    # each query's selection lives in one warp's shared-memory buffer: k+1 up
+    # to 16352 for float data, 8160 for double (checked before any device
+    # work: the tiny output buffers are never touched)
+    lib = _lib.load()
+    n = 20_000
+    x32 = np.zeros((n, 2), np.float32)
+    x64 = np.zeros((n, 2), np.float64)
+    ids = np.zeros(4, np.int32)
+    dd = np.zeros(4, np.float64)
+
+    def call(x, dt, k):
+        o = _lib.Options.make()
+        st = _lib.Stats.make()
+        return lib.knnsj_selfjoin(x.ctypes.data, dt, n, 2, k, ctypes.byref(o), ids.ctypes.data, dd.ctypes.data,
+                                  ctypes.byref(st))
+
+    assert call(x32, _lib.KNNSJ_F32, 16352) == 10
+    assert call(x64, _lib.KNNSJ_F64, 8160) == 10
+    assert call(x64, _lib.KNNSJ_F64, 16351) == 10
+
+
 def test_no_device_is_reported():
     torch = pytest.importorskip("torch")
     if torch.cuda.is_available():

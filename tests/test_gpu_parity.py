@@ -102,6 +102,16 @@ def test_k128_4d():
     gpu_vs_oracle(x, 128, 4, 0.05)
 
 
+@pytest.mark.parametrize("dtype,k", [(np.float32, 4095), (np.float32, 16351), (np.float64, 3000),
+                                     (np.float64, 8159)])
+def test_large_k(dtype, k):
+    # k+1 beyond 2048 (the reference has no cap on k): one warp per block
+    # with a selection buffer of up to 128 KB, the largest k+1 each type takes
+    n = max(12_000, k + 2_000)
+    x = datasets.gmm(n, 2, 6, 0.3, seed=k, dtype=dtype)
+    gpu_vs_oracle(x, k, 2, 0.0)
+
+
 def test_generic_dimension_path_d12():
     x = datasets.gmm(20_000, 12, 5, 0.3, seed=11, dtype=np.float32)
     gpu_vs_oracle(x, 8, 4, 0.05)
