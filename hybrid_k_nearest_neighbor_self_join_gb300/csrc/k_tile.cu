@@ -23,9 +23,9 @@
 //   3. the single pass over the candidates: every key (squared distance,
 //      id) within the query's radius goes to the query's list in shared
 //      memory, its slot from a ballot over the query's lanes (no atomics);
-//      a query that finds more keys than the list holds (about 1 %) is
-//      handed to search_kernel, one that finds fewer than K fails (the
-//      reference's acceptance rule, GPU.cu:3659-3669);
+//      a query that finds more keys than the list holds (0.2 % of the sky
+//      join) is handed to search_kernel, one that finds fewer than K fails
+//      (the reference's acceptance rule, GPU.cu:3659-3669);
 //   4. a histogram of the list in 128 bins of squared distance (a monotone
 //      map of [0, r^2]; 8-bit counts, four to a word, scanned bytewise),
 //      the bin holding the K-th smallest key and the count below it; a
